@@ -1,0 +1,196 @@
+/*
+ * tisphi_gb300 - C ABI of the GB300 (sm_103a) SPH step library.
+ *
+ * The reference (Rabmelon/tiSPHi) has no FFI layer: its hot path is a set of Taichi
+ * kernels reached through Python objects.  Each entry point below replaces one of those
+ * kernels (or one solver method that launches several); the comment on each names the
+ * reference interface it replaces (file:line inside the reference project).  The Python
+ * package tisphi_gb300 binds these through ctypes and mirrors the reference's object API
+ * (Simulation / ParticleSystem / SPHBase / WCSPHSolver / MUISPHSolver / DPSPHSolver).
+ *
+ * Conventions
+ *  - Every call that launches GPU work takes a CUDA stream (cudaStream_t passed as
+ *    void*; NULL = legacy default stream) and is asynchronous unless stated.
+ *  - Status: 0 = OK; > 0 = bits of the device error word (TSG_ERR_*); < 0 = API misuse or
+ *    a CUDA error (TSG_E_*).  No call aborts the process.
+ *  - Particle arrays handed to tsg_upload are row-major host or device arrays:
+ *    vectors (n, 3), matrices (n, 3, 3), scalars (n,).  All f64 / int32.
+ *  - The handle owns every device buffer; tsg_field returns a view that stays valid until
+ *    the next call that reorders particles (tsg_sort / tsg_step) or tsg_destroy.
+ */
+#ifndef TISPHI_GB300_H
+#define TISPHI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tsg_handle tsg_handle;
+
+/* precision forms */
+enum { TSG_FP64 = 0, TSG_FP32_MIXED = 1 };
+
+/* tsg_advect selectors */
+enum {
+    TSG_ADVECT_FULL = 1,       /* advect_SE / advect_LF (eng/solver_sph_base.py:79-87, :106-114) */
+    TSG_ADVECT_LF_HALF = 2,    /* advect_LF_half (eng/solver_sph_base.py:96-104) */
+    TSG_ADVECT_POS = 3,        /* advect_pos + XSPH (eng/solver_sph_base.py:224-238) */
+    TSG_ADVECT_SOMETHING = 4,  /* advect_something (eng/solver_sph_base.py:244-247 + solver overrides) */
+    TSG_ENFORCE_BOUNDARY = 5,  /* enforce_boundary (eng/solver_sph_base.py:525-601) */
+    TSG_RK_INIT = 6,           /* init_RK (eng/solver_sph_base.py:144-151) */
+    TSG_RK_STAGE = 7,          /* advect_RK_4 (eng/solver_sph_base.py:134-142) */
+    TSG_RK_FINAL = 8           /* advect_RK (eng/solver_sph_base.py:162-170) */
+};
+
+/* device error word bits */
+enum {
+    TSG_ERR_CELL_OOB = 1,      /* a particle's flattened cell index left [0, grid_num_total) */
+    TSG_ERR_NONFINITE = 2,     /* a non-finite density or position was produced */
+    TSG_ERR_PACK_RANGE = 4     /* FP32-mixed: a cell coordinate exceeded the packing range */
+};
+
+/* negative status codes */
+enum {
+    TSG_E_ARG = -1, TSG_E_CONFIG = -2, TSG_E_CUDA = -3, TSG_E_STATE = -4, TSG_E_UNSUPPORTED = -5,
+    TSG_E_NAME = -6, TSG_E_CAPACITY = -7
+};
+
+/* Scene and solver constants, as the reference's Python scope holds them
+ * (eng/particle_system.py:14-59, eng/solver_sph_base.py:12-26, solver constructors). */
+typedef struct tsg_config {
+    int32_t dim;               /* 2 or 3 */
+    int32_t solver;            /* 1 WCSPH, 2 mu(I), 3 Drucker-Prager (eng/simulation.py:14-22) */
+    int32_t kernel;            /* 0 cubic spline, 1 Wendland C2 */
+    int32_t kernel_corr;       /* 0 none, 1 CSPM */
+    int32_t time_integration;  /* 1 SE, 2 LF, 4 RK4 */
+    int32_t xsph;              /* 0 / 1 */
+    int32_t boundary;          /* 0 none, 1 collision, 2 dummy, 3 repulsive, 4 dummy + repulsive */
+    int32_t precision;         /* TSG_FP64 or TSG_FP32_MIXED */
+    int32_t exponent_is_int;   /* Tait exponent is an integer */
+    int32_t init_geostatic;    /* DP: apply init_stress on upload (eng/solver_sph_dp.py:35) */
+    int32_t grid_num[3];
+    int64_t grid_num_total;
+    double vdomain_start[3];
+    double domain_start[3];
+    double domain_end[3];
+    double grid_size;
+    double support_radius;
+    double smoothing_len;
+    double particle_diameter;
+    double particle_radius;
+    double gravity[3];
+    double dt;
+    double density0;
+    double viscosity;
+    double stiffness;
+    double exponent;
+    double cohesion;           /* Pa */
+    double friction;           /* rad */
+    double E;                  /* Young's modulus */
+    double poisson;
+    double dilatancy;          /* rad */
+    double damping_eps;        /* viscous damping coefficient (eng/solver_sph_base.py:714) */
+} tsg_config;
+
+/* Initial particle set (eng/particle_system.py:289-314 _add_particles). */
+typedef struct tsg_particles {
+    int64_t n;
+    const double* x;           /* (n, 3) */
+    const double* v;           /* (n, 3) */
+    const double* density;     /* (n,) */
+    const double* mass;        /* (n,) */
+    const double* m_V;         /* (n,) */
+    const double* pressure;    /* (n,) */
+    const double* stress;      /* (n, 3, 3) or NULL (zeros) */
+    const int32_t* mat_type;   /* -2 repulsive, -1 dummy, 1 fluid, 2 soil, 11 rigid */
+    const int32_t* mat_id;
+    const int32_t* obj_id;
+    const int32_t* is_dynamic;
+} tsg_particles;
+
+/* Strided view of one device field. */
+typedef struct tsg_view {
+    void* data;                /* device pointer */
+    int32_t dtype;             /* 0 f64, 1 f32, 2 i32 */
+    int32_t ndim;
+    int64_t shape[3];
+    int64_t strides[3];        /* in elements */
+} tsg_view;
+
+/* Create a solver instance.  Replaces ParticleSystem.__init__'s field allocation
+ * (eng/particle_system.py:113-125) and the solver constructors' constant set-up
+ * (eng/solver_sph_wc.py:7-21, eng/solver_sph_muI.py:7-25, eng/solver_sph_dp.py:7-35). */
+int tsg_create(const tsg_config* cfg, tsg_handle** out);
+
+/* Load the initial particles (host or device pointers, from_device = 0/1) and set
+ * id0 = index.  Replaces _add_particles + set_id0 (eng/particle_system.py:208-211,
+ * :289-314) and, for DP, init_stress (eng/solver_sph_base.py:249-260). */
+int tsg_upload(tsg_handle* h, const tsg_particles* p, int from_device, void* stream);
+
+/* Cell hash + prefix sum + stable counting sort.  Replaces initialize_particle_system
+ * (eng/particle_system.py:228-257). */
+int tsg_sort(tsg_handle* h, void* stream);
+
+/* Shepard factor for all particles and, when kernel_corr == 1, the CSPM gradient
+ * correction matrix.  Replaces calc_kernel_corr (eng/solver_sph_base.py:363-423). */
+int tsg_kernel_corr(tsg_handle* h, void* stream);
+
+/* density_tmp = density, v_tmp = v, stress_tmp = stress.  Replaces init_real2tmp
+ * (eng/solver_sph_base.py:67-74). */
+int tsg_init_tmp(tsg_handle* h, void* stream);
+
+/* One evaluation of the rates.  Replaces WCSPHSolver.one_step (eng/solver_sph_wc.py:82-127),
+ * MUISPHSolver.one_step (eng/solver_sph_muI.py:62-131) or DPSPHSolver.one_step
+ * (eng/solver_sph_dp.py:210-274), by the configured solver. */
+int tsg_one_step(tsg_handle* h, void* stream);
+
+/* Per-particle update selected by TSG_ADVECT_*; see the enum for the reference kernels. */
+int tsg_advect(tsg_handle* h, int which, void* stream);
+
+/* substep(): SE / LF / RK4 sequence of one_step and advect calls
+ * (eng/solver_sph_base.py:53-61, :89-91, :116-120, :172-180). */
+int tsg_substep(tsg_handle* h, void* stream);
+
+/* nsteps x SPHBase.step (eng/solver_sph_base.py:41-51). */
+int tsg_step(tsg_handle* h, int nsteps, void* stream);
+
+/* Device view of a named particle field in the current (cell-sorted) order.  Replaces
+ * attribute access on the reference's `pt` struct field (eng/particle_func.py:10-88).
+ * FP32-mixed instances return views of a f64 staging copy refreshed by this call. */
+int tsg_field(tsg_handle* h, const char* name, tsg_view* out, void* stream);
+
+/* Number of particles (ParticleSystem.particle_num[None], eng/particle_system.py:39). */
+int64_t tsg_particle_num(const tsg_handle* h);
+
+/* Cell offsets after the last sort: out[c] = inclusive end offset of cell c for
+ * c < grid_num_total, out[grid_num_total] = n (the trailing out-of-grid bin).  Mirrors
+ * grid_particle_num after the prefix sum (eng/particle_system.py:118, :256).  Host copy;
+ * synchronises the stream. */
+int tsg_grid(tsg_handle* h, int32_t* out, void* stream);
+
+/* Neighbour lists in the reference's traversal order (for_all_neighbors,
+ * eng/particle_system.py:259-269): counts[i] per particle and the concatenated indices.
+ * Host copies; synchronises.  *total receives the number of pairs; list may be NULL to
+ * query it; returns TSG_E_CAPACITY when cap is too small. */
+int tsg_neighbors(tsg_handle* h, int32_t* counts, int32_t* list, int64_t cap, int64_t* total, void* stream);
+
+/* FP64 diagnostics over flow particles: out[0] total mass, out[1..3] momentum,
+ * out[4] kinetic energy, out[5] potential energy (-m g.x), out[6] max |v|,
+ * out[7] max x of flow particles (front / runout).  No reference counterpart (the
+ * reference prints no conservation figures); synchronises. */
+int tsg_reduce_diag(tsg_handle* h, double out[8], void* stream);
+
+/* Device error word accumulated since the last call (and cleared).  Synchronises. */
+int tsg_last_error(tsg_handle* h, void* stream);
+
+/* Human-readable text for a status code. */
+const char* tsg_status_string(int status);
+
+void tsg_destroy(tsg_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TISPHI_GB300_H */
