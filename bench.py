@@ -1,0 +1,406 @@
+"""Benchmark: particle-updates/s of the 3D WCSPH dambreak step on one GB300.
+
+Workload (default): 3D WCSPH dambreak, domain 3.22 x 1.6 x 0.5 m, fluid block
+1.2 x 0.6 x 0.2 m at lattice spacing 0.0054 m (911,754 fluid + 1,413,114 dummy particles,
+2,324,868 total) with seeded +-1 % jitter, Wendland C2, Tait rho0 1000 / B 5e4 / gamma 7,
+viscosity 0.005, CSPM gradient correction on, XSPH off, leap-frog at dt = 2e-5.
+
+A "step" is one full ``SPHBase.step()``: cell sort, CSPM, two one_step evaluations with
+the half / full leap-frog updates, advect_pos and the density clamp.  particle-updates/s =
+fluid particles x steps / second.  The per-step working set (~0.5 GB) exceeds the 129 MB
+L2, so no flush is needed between steps.
+
+Printed (rank 0, one JSON line): ``value`` = the FP32-mixed form when the library provides
+it, else the FP64 form; the other form is reported beside it under ``forms``; ``e2e`` =
+the same metric through the public API with the step's inputs copied from pinned host
+memory and its results read back every step; ``roofline`` for the dominant kernel (the
+rates kernel), timed live with CUDA events; ``cpu_baseline`` = the f64 CPU oracle on the
+host cores for a bounded sample of the same workload.
+
+``--impl reference`` times the reference algorithm's CPU restatement (the oracle) instead,
+on all host cores, and prints the reference-arm line.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-updates/s, 1M 3D WCSPH: FP32-mixed vs plain FP64, 1 GB300, stated err"
+UNIT = "particle-updates/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+
+
+def workload(args):
+    from tisphi_gb300 import scenes
+    if args.workload == "3d":
+        return scenes.dambreak_3d(spacing=args.spacing), "3D WCSPH dambreak"
+    if args.workload == "2d":
+        return scenes.dambreak_2d(), "2D WCSPH dambreak"
+    raise SystemExit(f"unknown workload {args.workload}")
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+# ---------------------------------------------------------------- distributed plumbing
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend=backend)
+    return rank, ws, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, value):
+    if dist is None:
+        return value
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        loaded = [s for s in sm if smax and s > 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- CPU baseline (oracle)
+def cpu_baseline(cfg_dict, budget_s=25.0):
+    """f64 CPU oracle (the reference algorithm restated in C++/OpenMP) on the host cores."""
+    from oracle.oracle import OracleSim
+    from tisphi_gb300.configer_builder import SimConfiger
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    cfg = SimConfiger(config=cfg_dict)
+    orc = OracleSim(cfg)
+    n_fluid = int(np.count_nonzero(orc.scene.mat_type == 1))
+    t0 = time.perf_counter()
+    orc.step(1)
+    first = time.perf_counter() - t0
+    steps = 1
+    extra = max(0, min(4, int((budget_s - first) / max(first, 1e-3))))
+    if extra:
+        t1 = time.perf_counter()
+        orc.step(extra)
+        el = time.perf_counter() - t1
+        rate = n_fluid * extra / el
+        steps = extra
+    else:
+        rate = n_fluid / first
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} full step(s) of the same {orc.n:,}-particle scene after 1 untimed step, "
+                      f"f64 C++/OpenMP oracle, {cores} threads"}
+
+
+# ---------------------------------------------------------------- GPU measurement
+def algorithmic_bytes_rates(n_total, n_flow, precision, corr):
+    """Unique bytes the rates kernel must move once per launch (neighbour re-reads excluded).
+
+    FP64: every particle's x (24) + m_V (8) + v_tmp (24) + density_tmp (8) + pressure (8) +
+    mat_type (4) + f32 prefilter position (16) are read; each flow particle additionally
+    reads its list index (4) and CSPM matrix (72 when corrected) and writes d_density (8) and
+    d_vel (24).  FP32-mixed: position (16) + packed cell (4) + velocity/volume (16) +
+    density/pressure (8) per particle; per flow particle list (4) + CSPM (36 when corrected)
+    + writes (16).
+    """
+    if precision == "fp64":
+        return n_total * 92 + n_flow * (4 + (72 if corr else 0) + 32)
+    return n_total * 44 + n_flow * (4 + (36 if corr else 0) + 16)
+
+
+def measure(args, cfg_dict, precision, rank, dist):
+    import ctypes
+
+    import torch
+
+    from tisphi_gb300 import _native as nat
+    from tisphi_gb300.configer_builder import SimConfiger
+    from tisphi_gb300.simulation import Simulation
+
+    sim = Simulation(SimConfiger(config=cfg_dict), precision=precision)
+    ps, solver = sim.ps, sim.solver
+    lib = nat.load()
+    n_total = ps.particle_max_num
+    n_fluid = int(np.count_nonzero(ps.scene.mat_type == 1))
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        solver.step()
+    torch.cuda.synchronize()
+    ps.check_errors()
+    # ---- timed region: K steps, CUDA events on the launch stream
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        barrier(dist)
+        torch.cuda.synchronize()
+        l0 = lib.tsg_launch_count()
+        start.record(stream)
+        for _ in range(args.steps):
+            solver.step()
+        stop.record(stream)
+        torch.cuda.synchronize()
+        launches = lib.tsg_launch_count() - l0
+        barrier(dist)
+    ms = start.elapsed_time(stop) / args.steps
+    ms = max_over_ranks(dist, ms)
+    clocks = clk.summary()
+    ps.check_errors()
+    # ---- per-phase kernel timing (separate pass of the same steps, events on the stream)
+    lib.tsg_profile(1)
+    for _ in range(args.steps):
+        solver.step()
+    torch.cuda.synchronize()
+    nph = len(nat.PHASES)
+    pms = (ctypes.c_double * nph)()
+    pcnt = (ctypes.c_int64 * nph)()
+    lib.tsg_profile_read(pms, pcnt, nph)
+    lib.tsg_profile(0)
+    phases = {nat.PHASES[k]: {"ms_per_launch": (pms[k] / pcnt[k]) if pcnt[k] else 0.0,
+                              "launches": int(pcnt[k]), "share": pms[k] / max(sum(pms), 1e-12)}
+              for k in range(nph) if pcnt[k]}
+    # ---- end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        # The host owns the state between steps: every step writes x, v, density from pinned
+        # host memory and reads x, v, density, pressure back (in the order the step leaves).
+        host = {k: torch.empty((n_total, c), dtype=torch.float64).pin_memory()
+                for k, c in (("x", 3), ("v", 3), ("density", 1), ("pressure", 1))}
+        ins, outs = ("x", "v", "density"), ("x", "v", "density", "pressure")
+        for k in outs:
+            ps.read_field(k, host[k])
+        torch.cuda.synchronize()
+        e2e_steps = max(1, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for k in ins:
+                ps.write_field(k, host[k])
+            solver.step()
+            for k in outs:
+                ps.read_field(k, host[k])
+        torch.cuda.synchronize()
+        el = max_over_ranks(dist, time.perf_counter() - t0)
+        h2d = sum(host[k].numel() * 8 for k in ins)
+        d2h = sum(host[k].numel() * 8 for k in outs)
+        e2e = {"value": n_fluid * e2e_steps / el, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": e2e_steps}
+    diag = ps.diagnostics()
+    del sim
+    torch.cuda.synchronize()
+    return {"ms_per_step": ms, "value": n_fluid / (ms * 1e-3), "launches": launches,
+            "launches_per_step": launches / args.steps, "clocks": clocks, "phases": phases, "e2e": e2e,
+            "n_total": n_total, "n_fluid": n_fluid, "diag_mass": diag["mass"]}
+
+
+def read_profile_traffic(kernel_tag):
+    """Per-launch DRAM bytes from a committed ncu summary (profiles/*.md), or None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        return None
+    return None
+
+
+def run_ours(args):
+    import torch
+    rank, ws, dist = dist_init(args)
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    cfg_dict, wname = workload(args)
+    from tisphi_gb300 import build_native
+    build_native.build()
+    forms = {}
+    order = ["fp32_mixed", "fp64"] if args.precision == "both" else [args.precision]
+    for prec in order:
+        try:
+            forms[prec] = measure(args, cfg_dict, prec, rank, dist)
+        except Exception as e:  # FP32-mixed may be absent from the library build
+            forms[prec] = {"error": str(e)}
+    head = "fp32_mixed" if "value" in forms.get("fp32_mixed", {}) else "fp64"
+    h = forms[head]
+    if "value" not in h:
+        raise SystemExit(f"measurement failed: {forms}")
+    peak, peak_kind = hbm_peak()
+    corr = cfg_dict["Configuration"]["kernelCorrection"] == 1
+    n_flow = h["n_fluid"]
+    rates = h["phases"].get("rates", {"ms_per_launch": 0.0})
+    alg = algorithmic_bytes_rates(h["n_total"], n_flow, head, corr)
+    achieved = alg / (rates["ms_per_launch"] * 1e-3) / 1e9 if rates["ms_per_launch"] else 0.0
+    traffic = read_profile_traffic(f"rates_{head}_3d")
+    line = {
+        "metric": METRIC, "value": h["value"] * ws, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if head == "fp32_mixed" else "f64", "data": "synthetic",
+        "config": {"workload": f"{wname}, spacing {args.spacing} m, {h['n_fluid']:,} fluid + "
+                               f"{h['n_total'] - h['n_fluid']:,} dummy particles, LF dt 2e-5, CSPM on, XSPH off",
+                   "form": head, "n_fluid": h["n_fluid"], "n_total": h["n_total"],
+                   "l2": "working set > 129 MB L2 (no flush needed)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "forms": {k: ({"value": v["value"], "ms_per_step": v["ms_per_step"]} if "value" in v else v)
+                  for k, v in forms.items()},
+        "roofline": {"kernel": "rates (k_wc_rates)", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": rates["ms_per_launch"],
+                     "traffic": traffic},
+        "phases": h["phases"],
+        "clocks": h["clocks"],
+        "e2e": h["e2e"],
+        "gpu_launches": int(h["launches"]),
+    }
+    if "fp32_mixed" in forms and "fp64" in forms and "value" in forms["fp32_mixed"] and "value" in forms["fp64"]:
+        line["speedup_fp32_mixed_vs_fp64"] = forms["fp32_mixed"]["value"] / forms["fp64"]["value"]
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(cfg_dict)
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank, ws, dist = dist_init(args)
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    cfg_dict, wname = workload(args)
+    from oracle import oracle as orc_mod
+    orc_mod.build()
+    from oracle.oracle import OracleSim
+    from tisphi_gb300.configer_builder import SimConfiger
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    orc = OracleSim(SimConfiger(config=cfg_dict))
+    n_fluid = int(np.count_nonzero(orc.scene.mat_type == 1))
+    budget = 150.0
+    t0 = time.perf_counter()
+    orc.step(1)
+    first = time.perf_counter() - t0
+    warm = max(0, min(args.warmup - 1, int(budget * 0.2 / max(first, 1e-3))))
+    if warm:
+        orc.step(warm)
+    k = max(1, min(args.steps, int(budget * 0.6 / max(first, 1e-3))))
+    t1 = time.perf_counter()
+    orc.step(k)
+    el = time.perf_counter() - t1
+    v = n_fluid * k / el
+    sample = (f"{k} full step(s) of the {orc.n:,}-particle scene after {warm + 1} untimed, f64 C++/OpenMP "
+              f"restatement of the reference's Taichi kernels (Taichi itself is not installable here), "
+              f"{cores} threads")
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": k, "warmup": warm + 1,
+            "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"{wname}, spacing {args.spacing} m, {n_fluid:,} fluid + "
+                                   f"{orc.n - n_fluid:,} dummy particles", "form": "cpu-f64"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["both", "fp32_mixed", "fp64"], default="both")
+    ap.add_argument("--workload", choices=["3d", "2d"], default="3d")
+    ap.add_argument("--spacing", type=float, default=0.0054)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -185,6 +185,26 @@ int tsg_reduce_diag(tsg_handle* h, double out[8], void* stream);
 /* Device error word accumulated since the last call (and cleared).  Synchronises. */
 int tsg_last_error(tsg_handle* h, void* stream);
 
+/* Copy one named field between a caller buffer and the device state, in the current
+ * (cell-sorted) particle order.  The caller buffer is row-major (n, k) f64 for float fields
+ * and int32 for integer fields; host buffers should be pinned for the copies to overlap.
+ * Replaces the reference's from_numpy / to_numpy transfers (eng/particle_system.py:289-314,
+ * :413-456).  tsg_read synchronises the stream when the destination is on the host. */
+int tsg_write(tsg_handle* h, const char* name, const void* src, int from_device, void* stream);
+int tsg_read(tsg_handle* h, const char* name, void* dst, int to_device, void* stream);
+
+/* Number of kernel launches this library has issued since it was loaded (all handles).
+ * No reference counterpart: instrumentation for launch accounting. */
+int64_t tsg_launch_count(void);
+
+/* Per-phase CUDA-event timing (no reference counterpart; measurement only).  While enabled,
+ * every phase's kernels are bracketed by events on their launch stream.  tsg_profile_read
+ * synchronises the device, returns the summed milliseconds and bracket counts per phase
+ * (0 sort, 1 kernel correction, 2 init_tmp, 3 EOS / stress adaptation, 4 boundary
+ * extrapolation, 5 rates, 6 integration, 7 advect_pos, 8 post-step, 9 other) and clears. */
+int tsg_profile(int enable);
+int tsg_profile_read(double* ms, int64_t* counts, int nphase);
+
 /* Human-readable text for a status code. */
 const char* tsg_status_string(int status);
 

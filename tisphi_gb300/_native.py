@@ -15,6 +15,8 @@ TSG_FP64, TSG_FP32_MIXED = 0, 1
 TSG_ADVECT_FULL, TSG_ADVECT_LF_HALF, TSG_ADVECT_POS, TSG_ADVECT_SOMETHING, TSG_ENFORCE_BOUNDARY, \
     TSG_RK_INIT, TSG_RK_STAGE, TSG_RK_FINAL = range(1, 9)
 TSG_ERR_CELL_OOB, TSG_ERR_NONFINITE, TSG_ERR_PACK_RANGE = 1, 2, 4
+PHASES = ("sort", "kernel_corr", "init_tmp", "eos_adapt", "boundary", "rates", "integrate", "advect_pos",
+          "post", "other")
 
 
 class tsg_config(ctypes.Structure):
@@ -66,6 +68,11 @@ SYMBOLS = {
                                      ctypes.c_void_p]),
     "tsg_reduce_diag": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "tsg_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "tsg_write": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "tsg_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "tsg_launch_count": (ctypes.c_int64, []),
+    "tsg_profile": (ctypes.c_int, [ctypes.c_int]),
+    "tsg_profile_read": (ctypes.c_int, [_dp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "tsg_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "tsg_destroy": (None, [ctypes.c_void_p]),
 }

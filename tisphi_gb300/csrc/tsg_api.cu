@@ -1,6 +1,7 @@
 // C ABI of libtisphi_gb300: handle life cycle, uploads, the step sequence and field views.
 // The step sequence restates SPHBase.step / substep (eng/solver_sph_base.py:41-61,
 // :89-91, :116-120, :172-180) as a fixed list of kernel launches on one stream.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -12,6 +13,34 @@
 #include "tsg_fp32.h"
 
 using namespace tsg;
+
+namespace tsg {
+static std::atomic<long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+struct ProfRec { int phase; cudaEvent_t a, b; };
+struct Profiler {
+    bool on = false;
+    std::vector<ProfRec> recs;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t get() {
+        if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+        cudaEvent_t e; cudaEventCreate(&e); return e;
+    }
+};
+static Profiler g_prof;
+
+PhaseScope::PhaseScope(cudaStream_t s, int phase) : s_(s), phase_(phase), stop_(nullptr) {
+    if (!g_prof.on) return;
+    cudaEvent_t a = g_prof.get(), b = g_prof.get();
+    cudaEventRecord(a, s);
+    g_prof.recs.push_back({phase, a, b});
+    stop_ = reinterpret_cast<void*>(b);
+}
+PhaseScope::~PhaseScope() {
+    if (stop_) cudaEventRecord(reinterpret_cast<cudaEvent_t>(stop_), s_);
+}
+}  // namespace tsg
 
 struct tsg_handle {
     tsg_config cfg;
@@ -124,7 +153,7 @@ int upload_planes(tsg_handle* h, const double* src, double* dst, int k, bool fro
     if (!src) { cudaMemsetAsync(dst, 0, bytes, s); return 0; }
     cudaMemcpyAsync(h->d_stage, src, bytes, from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
     if (k == 1) cudaMemcpyAsync(dst, h->d_stage, bytes, cudaMemcpyDeviceToDevice, s);
-    else k_deinterleave<<<nb256(h->n), 256, 0, s>>>(h->d_stage, dst, h->n, k);
+    else TSG_LAUNCH(k_deinterleave, nb256(h->n), 256, s, h->d_stage, dst, h->n, k);
     return 0;
 }
 
@@ -297,7 +326,7 @@ int tsg_upload(tsg_handle* h, const tsg_particles* p, int from_device, void* str
     upload_ints(p->mat_id, h->cur.mat_id, h->n, dev, s);
     upload_ints(p->obj_id, h->cur.obj_id, h->n, dev, s);
     upload_ints(p->is_dynamic, h->cur.is_dynamic, h->n, dev, s);
-    k_iota<<<nb256(h->n), 256, 0, s>>>(h->cur.id0, h->n);
+    TSG_LAUNCH(k_iota, nb256(h->n), 256, s, h->cur.id0, h->n);
     if (c.solver == 3 && h->cfg.init_geostatic) fp64_init_geostatic(c, h->cur, h->d_scratch, s);
     h->uploaded = true;
     h->pos32_dirty = true;
@@ -452,6 +481,89 @@ int tsg_field(tsg_handle* h, const char* name, tsg_view* out, void* stream) {
         out->strides[0] = 1; out->strides[1] = 3 * n; out->strides[2] = n;
     }
     return 0;
+}
+
+namespace {
+
+__global__ void k_interleave(const double* __restrict__ src, double* __restrict__ dst, int n, int k) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int q = 0; q < k; ++q) dst[(size_t)i * k + q] = src[(size_t)q * n + i];
+}
+
+// Planar device field behind a name for tsg_write / tsg_read (FP64 form).
+int planar_field(tsg_handle* h, const std::string& f, void** ptr, int* comps, int* is_int) {
+    tsg_view v;
+    int rc = tsg_field(h, f.c_str(), &v, nullptr);
+    if (rc) return rc;
+    *ptr = v.data;
+    *comps = v.ndim == 1 ? 1 : (v.ndim == 2 ? 3 : 9);
+    *is_int = v.dtype == 2;
+    return 0;
+}
+
+}  // namespace
+
+int tsg_write(tsg_handle* h, const char* name, const void* src, int from_device, void* stream) {
+    if (!h || !name || !src || !h->uploaded) return TSG_E_ARG;
+    cudaStream_t s = S(stream);
+    if (use_fp32(h)) return fp32_write(*h->f32, name, src, from_device != 0, s);
+    void* ptr;
+    int comps, is_int;
+    int rc = planar_field(h, name, &ptr, &comps, &is_int);
+    if (rc) return rc;
+    const size_t n = h->n;
+    if (is_int) {
+        cudaMemcpyAsync(ptr, src, sizeof(int) * n, from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
+    } else {
+        upload_planes(h, static_cast<const double*>(src), static_cast<double*>(ptr), comps, from_device != 0, s);
+    }
+    if (std::string(name) == "x") h->pos32_dirty = true;
+    return check_cuda();
+}
+
+int tsg_read(tsg_handle* h, const char* name, void* dst, int to_device, void* stream) {
+    if (!h || !name || !dst || !h->uploaded) return TSG_E_ARG;
+    cudaStream_t s = S(stream);
+    if (use_fp32(h)) return fp32_read(*h->f32, name, dst, to_device != 0, s);
+    void* ptr;
+    int comps, is_int;
+    int rc = planar_field(h, name, &ptr, &comps, &is_int);
+    if (rc) return rc;
+    const size_t n = h->n;
+    const cudaMemcpyKind kind = to_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (is_int) {
+        cudaMemcpyAsync(dst, ptr, sizeof(int) * n, kind, s);
+    } else if (comps == 1) {
+        cudaMemcpyAsync(dst, ptr, sizeof(double) * n, kind, s);
+    } else {
+        TSG_LAUNCH(k_interleave, nb256(n), 256, s, static_cast<const double*>(ptr), h->d_stage, (int)n, comps);
+        cudaMemcpyAsync(dst, h->d_stage, sizeof(double) * n * comps, kind, s);
+    }
+    if (!to_device) cudaStreamSynchronize(s);
+    return check_cuda();
+}
+
+int64_t tsg_launch_count(void) { return tsg::g_launches.load(); }
+
+int tsg_profile(int enable) {
+    tsg::g_prof.on = enable != 0;
+    return 0;
+}
+
+int tsg_profile_read(double* ms, int64_t* counts, int nphase) {
+    if (!ms || !counts || nphase <= 0) return TSG_E_ARG;
+    for (int k = 0; k < nphase; ++k) { ms[k] = 0.0; counts[k] = 0; }
+    cudaDeviceSynchronize();
+    for (auto& r : tsg::g_prof.recs) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, r.a, r.b);
+        if (r.phase < nphase) { ms[r.phase] += t; counts[r.phase] += 1; }
+        tsg::g_prof.pool.push_back(r.a);
+        tsg::g_prof.pool.push_back(r.b);
+    }
+    tsg::g_prof.recs.clear();
+    return check_cuda();
 }
 
 int tsg_grid(tsg_handle* h, int32_t* out, void* stream) {

@@ -21,5 +21,7 @@ const int* fp32_cell_start(const Fp32State&) { return nullptr; }
 void fp32_neighbors(Fp32State&, int*, int*, int*, cudaStream_t) {}
 void fp32_diag(Fp32State&, double*, double*, cudaStream_t) {}
 int* fp32_err_ptr(Fp32State& st) { return &st.err; }
+int fp32_write(Fp32State&, const char*, const void*, bool, cudaStream_t) { return TSG_E_UNSUPPORTED; }
+int fp32_read(Fp32State&, const char*, void*, bool, cudaStream_t) { return TSG_E_UNSUPPORTED; }
 
 }  // namespace tsg

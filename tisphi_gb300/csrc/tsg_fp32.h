@@ -20,5 +20,7 @@ const int* fp32_cell_start(const Fp32State& st);
 void fp32_neighbors(Fp32State& st, int* counts, int* offsets, int* list, cudaStream_t s);
 void fp32_diag(Fp32State& st, double* scratch, double* host_out8, cudaStream_t s);
 int* fp32_err_ptr(Fp32State& st);
+int fp32_write(Fp32State& st, const char* name, const void* src, bool from_device, cudaStream_t s);
+int fp32_read(Fp32State& st, const char* name, void* dst, bool to_device, cudaStream_t s);
 
 }  // namespace tsg

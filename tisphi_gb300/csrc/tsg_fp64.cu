@@ -946,26 +946,35 @@ __global__ void k_ymax_soil(Consts c, Persist64 p, double* out) {
 // ---------------------------------------------------------------- launchers
 #define DISPATCH_DIM(c, KERNEL, GRID, ...)                                   \
     do {                                                                     \
-        if ((c).dim == 2) KERNEL<2><<<GRID, TPB, 0, s>>>(__VA_ARGS__);       \
-        else KERNEL<3><<<GRID, TPB, 0, s>>>(__VA_ARGS__);                    \
+        if ((c).dim == 2) TSG_LAUNCH(KERNEL<2>, GRID, TPB, s, __VA_ARGS__);       \
+        else TSG_LAUNCH(KERNEL<3>, GRID, TPB, s, __VA_ARGS__);                    \
     } while (0)
 
 void fp64_kernel_corr(const Consts& c, const Persist64& p, Trans64& t, const Grid& g, cudaStream_t s) {
+    PhaseScope ph(s, PH_CORR);
     DISPATCH_DIM(c, k_corr, nblk(c.n), c, p, t, g.cell_start);
 }
 
 void fp64_init_tmp(const Consts& c, const Persist64& p, Trans64& t, cudaStream_t s) {
-    k_init_tmp<<<nblk(c.n), TPB, 0, s>>>(c, p, t);
+    PhaseScope ph(s, PH_INIT);
+    TSG_LAUNCH(k_init_tmp, nblk(c.n), TPB, s, c, p, t);
 }
 
 void fp64_one_step(const Consts& c, Persist64& p, Trans64& t, const Grid& g, cudaStream_t s) {
-    if (c.n_flow > 0 && (c.solver == 1 || c.solver == 3))
-        k_pre<<<nblk(c.n_flow), TPB, 0, s>>>(c, p, t, g.list_flow, c.n_flow);
-    if (c.solver == 2 && c.n_flow > 0)
+    if (c.n_flow > 0 && (c.solver == 1 || c.solver == 3)) {
+        PhaseScope ph(s, PH_PRE);
+        TSG_LAUNCH(k_pre, nblk(c.n_flow), TPB, s, c, p, t, g.list_flow, c.n_flow);
+    }
+    if (c.solver == 2 && c.n_flow > 0) {
+        PhaseScope ph(s, PH_PRE);
         DISPATCH_DIM(c, k_mui_stress, nblk(c.n_flow), c, p, t, g.cell_start, g.list_flow, c.n_flow);
-    if (c.n_bdy > 0)
+    }
+    if (c.n_bdy > 0) {
+        PhaseScope ph(s, PH_BDY);
         DISPATCH_DIM(c, k_bdy, nblk(c.n_bdy), c, p, t, g.cell_start, g.list_bdy, c.n_bdy);
+    }
     if (c.n_flow > 0) {
+        PhaseScope ph(s, PH_RATES);
         if (c.solver == 1) DISPATCH_DIM(c, k_wc_rates, nblk(c.n_flow), c, p, t, g.cell_start, g.list_flow, c.n_flow);
         else if (c.solver == 2) DISPATCH_DIM(c, k_mui_mom, nblk(c.n_flow), c, p, t, g.cell_start, g.list_flow, c.n_flow);
         else DISPATCH_DIM(c, k_dp_rates, nblk(c.n_flow), c, p, t, g.cell_start, g.list_flow, c.n_flow);
@@ -974,31 +983,34 @@ void fp64_one_step(const Consts& c, Persist64& p, Trans64& t, const Grid& g, cud
 
 void fp64_advect(const Consts& c, Persist64& p, Trans64& t, const Grid& g, int which, cudaStream_t s) {
     const int nb = nblk(c.n);
+    PhaseScope ph(s, which == TSG_ADVECT_POS ? PH_POS : which == TSG_ADVECT_SOMETHING ? PH_POST
+                     : which == TSG_ENFORCE_BOUNDARY ? PH_OTHER : PH_INTEGRATE);
     switch (which) {
-    case TSG_ADVECT_FULL: k_advect_full<<<nb, TPB, 0, s>>>(c, p, t, g.err); break;
-    case TSG_ADVECT_LF_HALF: k_advect_half<<<nb, TPB, 0, s>>>(c, p, t); break;
+    case TSG_ADVECT_FULL: TSG_LAUNCH(k_advect_full, nb, TPB, s, c, p, t, g.err); break;
+    case TSG_ADVECT_LF_HALF: TSG_LAUNCH(k_advect_half, nb, TPB, s, c, p, t); break;
     case TSG_ADVECT_POS:
         if (c.xsph) DISPATCH_DIM(c, k_xsph, nb, c, p, t, g.cell_start);
-        k_advect_pos<<<nb, TPB, 0, s>>>(c, p, t, g.err);
+        TSG_LAUNCH(k_advect_pos, nb, TPB, s, c, p, t, g.err);
         break;
     case TSG_ADVECT_SOMETHING:
-        if (c.solver == 1) k_post_wc<<<nb, TPB, 0, s>>>(c, p);
+        if (c.solver == 1) TSG_LAUNCH(k_post_wc, nb, TPB, s, c, p);
         else if (c.solver == 2) {
-            k_post_mui_a<<<nb, TPB, 0, s>>>(c, p, t);
+            TSG_LAUNCH(k_post_mui_a, nb, TPB, s, c, p, t);
             DISPATCH_DIM(c, k_post_mui_b, nb, c, p, t, g.cell_start);
-            k_post_mui_c<<<nb, TPB, 0, s>>>(c, p, t);
-        } else k_post_dp<<<nb, TPB, 0, s>>>(c, p, t);
+            TSG_LAUNCH(k_post_mui_c, nb, TPB, s, c, p, t);
+        } else TSG_LAUNCH(k_post_dp, nb, TPB, s, c, p, t);
         break;
-    case TSG_ENFORCE_BOUNDARY: k_enforce<<<nb, TPB, 0, s>>>(c, p); break;
-    case TSG_RK_INIT: k_rk_init<<<nb, TPB, 0, s>>>(c, p, t); break;
-    case TSG_RK_STAGE: k_rk_stage<<<nb, TPB, 0, s>>>(c, p, t); break;
-    case TSG_RK_FINAL: k_rk_final<<<nb, TPB, 0, s>>>(c, p, t, g.err); break;
+    case TSG_ENFORCE_BOUNDARY: TSG_LAUNCH(k_enforce, nb, TPB, s, c, p); break;
+    case TSG_RK_INIT: TSG_LAUNCH(k_rk_init, nb, TPB, s, c, p, t); break;
+    case TSG_RK_STAGE: TSG_LAUNCH(k_rk_stage, nb, TPB, s, c, p, t); break;
+    case TSG_RK_FINAL: TSG_LAUNCH(k_rk_final, nb, TPB, s, c, p, t, g.err); break;
     default: break;
     }
 }
 
 void fp64_rk_update(const Consts& c, Persist64& p, Trans64& t, int m, cudaStream_t s) {
-    k_rk_update<<<nblk(c.n), TPB, 0, s>>>(c, p, t, m);
+    PhaseScope ph(s, PH_INTEGRATE);
+    TSG_LAUNCH(k_rk_update, nblk(c.n), TPB, s, c, p, t, m);
 }
 
 void fp64_neighbors(const Consts& c, const Persist64& p, const Trans64& t, const Grid& g,
@@ -1014,15 +1026,15 @@ void fp64_diag(const Consts& c, const Persist64& p, double* out8, cudaStream_t s
     double init[8] = {0, 0, 0, 0, 0, 0, 0, -DBL_MAX};
     cudaMemcpyAsync(out8, init, sizeof init, cudaMemcpyHostToDevice, s);
     cudaStreamSynchronize(s);
-    k_diag<<<nblk(c.n), TPB, 0, s>>>(c, p, out8);
+    TSG_LAUNCH(k_diag, nblk(c.n), TPB, s, c, p, out8);
 }
 
 void fp64_init_geostatic(const Consts& c, Persist64& p, double* scratch, cudaStream_t s) {
     double init = -DBL_MAX;
     cudaMemcpyAsync(scratch, &init, sizeof init, cudaMemcpyHostToDevice, s);
     cudaStreamSynchronize(s);
-    k_ymax_soil<<<nblk(c.n), TPB, 0, s>>>(c, p, scratch);
-    k_geostatic<<<nblk(c.n), TPB, 0, s>>>(c, p, scratch, c.K0);
+    TSG_LAUNCH(k_ymax_soil, nblk(c.n), TPB, s, c, p, scratch);
+    TSG_LAUNCH(k_geostatic, nblk(c.n), TPB, s, c, p, scratch, c.K0);
 }
 
 __global__ void k_refresh_pos32_impl(Consts c, const double* __restrict__ x, float4* __restrict__ pos32) {
@@ -1033,7 +1045,7 @@ __global__ void k_refresh_pos32_impl(Consts c, const double* __restrict__ x, flo
 }
 
 void fp64_refresh_pos32(const Consts& c, const Persist64& p, Trans64& t, cudaStream_t s) {
-    k_refresh_pos32_impl<<<nblk(c.n), TPB, 0, s>>>(c, p.x, t.pos32);
+    TSG_LAUNCH(k_refresh_pos32_impl, nblk(c.n), TPB, s, c, p.x, t.pos32);
 }
 
 }  // namespace tsg

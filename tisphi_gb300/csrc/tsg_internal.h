@@ -7,6 +7,25 @@
 
 namespace tsg {
 
+// Host-side count of kernel launches issued by this library (all handles).
+void note_launch();
+#define TSG_LAUNCH(kernel, grid, block, stream, ...)                   \
+    do {                                                                \
+        ::tsg::note_launch();                                           \
+        kernel<<<(grid), (block), 0, (stream)>>>(__VA_ARGS__);          \
+    } while (0)
+
+// Phase profiling: when enabled, every launcher brackets its kernels with CUDA events
+// recorded on the launching stream, and elapsed times are summed per phase.
+enum Phase { PH_SORT = 0, PH_CORR, PH_INIT, PH_PRE, PH_BDY, PH_RATES, PH_INTEGRATE, PH_POS, PH_POST, PH_OTHER, PH_COUNT };
+struct PhaseScope {
+    PhaseScope(cudaStream_t s, int phase);
+    ~PhaseScope();
+    cudaStream_t s_;
+    int phase_;
+    void* stop_;
+};
+
 constexpr int MAT_REP = -2, MAT_DUMMY = -1, MAT_FLUID = 1, MAT_SOIL = 2, MAT_RIGID = 11;
 constexpr double EPS = 1e-8;      // SPHBase.epsilon (eng/solver_sph_base.py:25)
 constexpr double EPS_F = 1e-4;    // DPSPHSolver.eps_f (eng/solver_sph_dp.py:23)

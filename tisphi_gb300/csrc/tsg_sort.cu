@@ -198,23 +198,24 @@ inline int nblk(long long n) { return (int)((n + TPB - 1) / TPB); }
 
 void scan_exclusive(const int* in, int* out, int n, int* tile_sum, cudaStream_t s) {
     int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
-    k_tile_sums<<<ntiles, TPB, 0, s>>>(in, n, tile_sum);
-    k_scan_tiles<<<1, TPB, 0, s>>>(tile_sum, ntiles);
-    k_tile_rescan<<<ntiles, TPB, 0, s>>>(in, n, tile_sum, out);
+    TSG_LAUNCH(k_tile_sums, ntiles, TPB, s, in, n, tile_sum);
+    TSG_LAUNCH(k_scan_tiles, 1, TPB, s, tile_sum, ntiles);
+    TSG_LAUNCH(k_tile_rescan, ntiles, TPB, s, in, n, tile_sum, out);
 }
 
 void sort_fp64(const Consts& c, Persist64& cur, Persist64& nxt, Trans64& t, Grid& g, cudaStream_t s) {
+    PhaseScope ph(s, PH_SORT);
     const long long nbins = c.G + 1;
     cudaMemsetAsync(g.count, 0, sizeof(int) * nbins, s);
     cudaMemsetAsync(g.list_count, 0, sizeof(int) * 2, s);
-    k_hash<<<nblk(c.n), TPB, 0, s>>>(c, cur.x, g.cell_of, g.rank, g.count, g.err);
+    TSG_LAUNCH(k_hash, nblk(c.n), TPB, s, c, cur.x, g.cell_of, g.rank, g.count, g.err);
     scan_exclusive(g.count, g.cell_start, (int)nbins, g.tile_sum, s);
-    k_scatter<<<nblk(c.n), TPB, 0, s>>>(c.n, g.cell_of, g.rank, g.cell_start, g.perm);
-    k_cell_sort<<<nblk(nbins), TPB, 0, s>>>(nbins, g.cell_start, g.perm);
+    TSG_LAUNCH(k_scatter, nblk(c.n), TPB, s, c.n, g.cell_of, g.rank, g.cell_start, g.perm);
+    TSG_LAUNCH(k_cell_sort, nblk(nbins), TPB, s, nbins, g.cell_start, g.perm);
     if (c.solver == 1)
-        k_reorder64<false><<<nblk(c.n), TPB, 0, s>>>(c, g.perm, cur, nxt, t.pos32, g.list_flow, g.list_bdy, g.list_count);
+        TSG_LAUNCH(k_reorder64<false>, nblk(c.n), TPB, s, c, g.perm, cur, nxt, t.pos32, g.list_flow, g.list_bdy, g.list_count);
     else
-        k_reorder64<true><<<nblk(c.n), TPB, 0, s>>>(c, g.perm, cur, nxt, t.pos32, g.list_flow, g.list_bdy, g.list_count);
+        TSG_LAUNCH(k_reorder64<true>, nblk(c.n), TPB, s, c, g.perm, cur, nxt, t.pos32, g.list_flow, g.list_bdy, g.list_count);
     Persist64 tmp = cur;
     cur = nxt;
     nxt = tmp;

@@ -130,6 +130,27 @@ class ParticleSystem:
         nat.check(self._lib.tsg_field(self._h, name.encode(), ctypes.byref(v), _stream()), f"field {name}")
         return torch.as_tensor(nat.DeviceArray(v, self), device="cuda")
 
+    def write_field(self, name, src):
+        """Copy a row-major (n, k) buffer (numpy array or torch tensor, host or CUDA) into a field."""
+        if isinstance(src, torch.Tensor):
+            assert src.is_contiguous()
+            ptr, dev = src.data_ptr(), int(src.is_cuda)
+        else:
+            src = np.ascontiguousarray(src)
+            ptr, dev = src.ctypes.data, 0
+        nat.check(self._lib.tsg_write(self._h, name.encode(), ctypes.c_void_p(ptr), dev, _stream()), f"write {name}")
+
+    def read_field(self, name, dst):
+        """Copy a field into a row-major (n, k) buffer (numpy array or torch tensor, host or CUDA)."""
+        if isinstance(dst, torch.Tensor):
+            assert dst.is_contiguous()
+            ptr, dev = dst.data_ptr(), int(dst.is_cuda)
+        else:
+            assert dst.flags.c_contiguous
+            ptr, dev = dst.ctypes.data, 0
+        nat.check(self._lib.tsg_read(self._h, name.encode(), ctypes.c_void_p(ptr), dev, _stream()), f"read {name}")
+        return dst
+
     @property
     def grid_particle_num(self):
         """Inclusive end offset of every cell after the last sort (host numpy, int32)."""
