@@ -1,0 +1,134 @@
+"""FP32-mixed GPU form vs the f64 CPU oracle, with stated tolerances.
+
+The FP32-mixed form keeps real particles and static boundary particles in separate
+cell-sorted blocks, so every comparison matches particles through id0.  Tolerances:
+
+* neighbour sets: identical, except pairs whose f64 distance is within 1e-6 R of the
+  support radius (f32 positions decide those; the kernel weight there is ~1e-20 of peak);
+* single-step rates (CSPM factor, d_density, d_vel): normwise relative error <= 1e-4;
+* density after a few steps: relative error <= 1e-5 (the headline accuracy bound);
+* positions after a few steps: absolute error <= 1e-6 m.
+"""
+import numpy as np
+import pytest
+
+from helpers import cfg_of, small_dambreak_2d, small_dambreak_3d
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(d, oracle_lib):
+    from tisphi_gb300.simulation import Simulation
+    cfg = cfg_of(d)
+    sim = Simulation(cfg, precision="fp32_mixed")
+    orc = oracle_lib.OracleSim(cfg)
+    return sim, orc
+
+
+def _by_id(sim, orc, name):
+    """GPU field re-ordered to the oracle's current order (through id0)."""
+    gid = sim.ps.field("id0").cpu().numpy()
+    oid = orc.get("id0").astype(np.int64)
+    a = sim.ps.field(name).cpu().numpy().astype(np.float64)
+    inv = np.empty_like(gid)
+    inv[gid] = np.arange(gid.size)
+    return a[inv[oid]]
+
+
+def _normwise(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def _advance(sim, orc, oracle_lib, steps):
+    sim.solver.step(steps)
+    orc.step(steps)
+
+
+@pytest.mark.parametrize("scene", ["2d", "3d"])
+def test_neighbor_sets_match(oracle_lib, native, scene):
+    d = small_dambreak_2d() if scene == "2d" else small_dambreak_3d()
+    sim, orc = _pair(d, oracle_lib)
+    sim.ps.initialize_particle_system()
+    orc.sort()
+    gc, gl = sim.ps.neighbors()
+    oc, ol = orc.neighbors()
+    gid = sim.ps.field("id0").cpu().numpy()
+    oid = orc.get("id0").astype(np.int64)
+    mt = orc.get("mat_type").astype(np.int64)
+    x = orc.get("x")
+    R = sim.ps.support_radius
+    goff = np.concatenate([[0], np.cumsum(gc)])
+    ooff = np.concatenate([[0], np.cumsum(oc)])
+    g_of_id = {int(gid[k]): k for k in range(gid.size)}
+    flow_ids = set(oid[(mt == 1) | (mt == 2)].tolist())
+    mismatched = 0
+    for oi in range(oid.size):
+        gk = g_of_id[int(oid[oi])]
+        gset = set(gid[gl[goff[gk]:goff[gk + 1]]].tolist())
+        oset = set(oid[ol[ooff[oi]:ooff[oi + 1]]].tolist())
+        if mt[oi] not in (1, 2):
+            oset &= flow_ids  # boundary particles list flow neighbours only
+        for idn in gset ^ oset:
+            oj = int(np.nonzero(oid == idn)[0][0])
+            r = np.linalg.norm(x[oi] - x[oj])
+            assert abs(r - R) < 1e-6 * R, f"pair ({oid[oi]}, {idn}) at r={r} differs"
+            mismatched += 1
+    assert mismatched <= 4
+
+
+def test_kernel_corr_close(oracle_lib, native):
+    sim, orc = _pair(small_dambreak_3d(corr=1), oracle_lib)
+    sim.ps.initialize_particle_system()
+    orc.sort()
+    sim.solver.calc_kernel_corr()
+    orc.call(oracle_lib.ORC_KERNEL_CORR)
+    assert _normwise(_by_id(sim, orc, "CSPM_f"), orc.get("CSPM_f")) < 1e-5
+    mt = orc.get("mat_type")
+    L = _by_id(sim, orc, "CSPM_L")
+    Lo = orc.get("CSPM_L")
+    f = mt == 1
+    assert _normwise(L[f], Lo[f]) < 1e-4
+
+
+@pytest.mark.parametrize("scene,corr", [("2d", 0), ("3d", 1)])
+def test_one_step_rates_close(oracle_lib, native, scene, corr):
+    d = small_dambreak_2d(corr=corr) if scene == "2d" else small_dambreak_3d(corr=corr)
+    sim, orc = _pair(d, oracle_lib)
+    _advance(sim, orc, oracle_lib, 3)
+    sim.ps.initialize_particle_system()
+    orc.sort()
+    sim.solver.calc_kernel_corr()
+    orc.call(oracle_lib.ORC_KERNEL_CORR)
+    sim.solver.init_real2tmp()
+    orc.call(oracle_lib.ORC_INIT_TMP)
+    sim.solver.one_step()
+    orc.call(oracle_lib.ORC_ONE_STEP)
+    f = orc.get("mat_type") == 1
+    for name in ("d_density", "d_vel", "pressure"):
+        err = _normwise(_by_id(sim, orc, name)[f], orc.get(name)[f])
+        assert err < 1e-4, f"{name}: normwise error {err:.3e}"
+
+
+@pytest.mark.parametrize("scene,ti", [("2d", 2), ("2d", 1), ("3d", 2)])
+def test_steps_density_position(oracle_lib, native, scene, ti):
+    d = small_dambreak_2d(integration=ti) if scene == "2d" else small_dambreak_3d(integration=ti)
+    sim, orc = _pair(d, oracle_lib)
+    _advance(sim, orc, oracle_lib, 10)
+    f = orc.get("mat_type") == 1
+    rho = _by_id(sim, orc, "density")[f]
+    rho_o = orc.get("density")[f]
+    assert np.max(np.abs(rho - rho_o) / rho_o) < 1e-5
+    x = _by_id(sim, orc, "x")[f]
+    assert np.max(np.abs(x - orc.get("x")[f])) < 1e-6
+    sim.ps.check_errors()
+
+
+def test_fp32_determinism(oracle_lib, native):
+    from tisphi_gb300.simulation import Simulation
+    d = small_dambreak_2d()
+    a = Simulation(cfg_of(d), precision="fp32_mixed")
+    b = Simulation(cfg_of(d), precision="fp32_mixed")
+    a.solver.step(10)
+    b.solver.step(10)
+    for nm in ("x", "v", "density"):
+        np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy())
