@@ -23,6 +23,8 @@ def _cfg(**kw):
         "gravitation": [0.0, -9.81, 0.0], "particleRadius": 0.005, "kappa": 2.0, "kh": 1.5,
         "simulationMethod": 1, "timeStepSizeMin": 1e-4, "boundary": 2, "kernel": 1,
         "kernelCorrection": 0, "timeIntegration": 2, "xsph": False,
+        # presentation keys of the scene schema (read by the reference's constructors)
+        "colorTitle": 2, "colorGroup": 0, "showBdyPts": False, "stepsPerRenderUpdate": 10,
     }
     base.update(kw)
     return base
