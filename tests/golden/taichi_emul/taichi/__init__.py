@@ -756,6 +756,12 @@ def __ti_loop(key, it):
     return fn(seq)
 
 
+def call_with_refs(f, *args):
+    """Call a ti.func from Python scope with template arguments passed by reference;
+    returns the final values of all arguments (boxed values are unboxed)."""
+    return __ti_call(f, *args)
+
+
 _HELPERS = {"__ti_deref": __ti_deref, "__ti_aug": __ti_aug, "__ti_call": __ti_call, "__ti_atomic": __ti_atomic,
             "__ti_atomic_local": __ti_atomic_local, "__ti_setsub": __ti_setsub, "__ti_loop": __ti_loop}
 
