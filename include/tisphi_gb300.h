@@ -205,6 +205,26 @@ int64_t tsg_launch_count(void);
 int tsg_profile(int enable);
 int tsg_profile_read(double* ms, int64_t* counts, int nphase);
 
+/* Allocation-free cell-list sort.  No counterpart in the reference: it serves callers
+ * that cannot call cudaMalloc - code whose device memory is planned up front by a
+ * fixed-budget pool or another framework's allocator, and stepping loops that must not
+ * risk the device-wide synchronisation cudaMalloc / cudaFree can cause.  It performs the
+ * same stable counting sort as tsg_sort on caller-owned buffers: x is a device array of
+ * n positions, row-major (n, 3) f64; the grid comes from cfg (vdomain_start, grid_size,
+ * grid_num, grid_num_total).  Outputs, both on the device: cell_start (grid_num_total + 2
+ * ints; cell c holds new positions [cell_start[c], cell_start[c + 1]), the last bin holds
+ * particles outside the grid) and perm (n ints; new position -> index into x).
+ * It allocates nothing: its scratch lives in fixed file-scope device arrays (about 3 MB
+ * per GPU, held until the process exits), so n must not exceed TSG_NOALLOC_MAX_PARTICLES
+ * and grid_num_total + 1 must not exceed TSG_NOALLOC_MAX_CELLS (else TSG_E_CAPACITY).
+ * Every call shares that scratch, so calls that overlap on the GPU race.  The first call
+ * on a device looks up the scratch address (once per device); make it before any stream
+ * capture begins. */
+#define TSG_NOALLOC_MAX_PARTICLES 262144
+#define TSG_NOALLOC_MAX_CELLS 262144
+int tsg_sort_noalloc(const tsg_config* cfg, const double* x, int64_t n, int32_t* cell_start, int32_t* perm,
+                     void* stream);
+
 /* Human-readable text for a status code. */
 const char* tsg_status_string(int status);
 

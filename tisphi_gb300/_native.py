@@ -73,6 +73,8 @@ SYMBOLS = {
     "tsg_launch_count": (ctypes.c_int64, []),
     "tsg_profile": (ctypes.c_int, [ctypes.c_int]),
     "tsg_profile_read": (ctypes.c_int, [_dp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
+    "tsg_sort_noalloc": (ctypes.c_int, [ctypes.POINTER(tsg_config), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p]),
     "tsg_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "tsg_destroy": (None, [ctypes.c_void_p]),
 }
