@@ -201,7 +201,8 @@ int64_t tsg_launch_count(void);
  * every phase's kernels are bracketed by events on their launch stream.  tsg_profile_read
  * synchronises the device, returns the summed milliseconds and bracket counts per phase
  * (0 sort, 1 kernel correction, 2 init_tmp, 3 EOS / stress adaptation, 4 boundary
- * extrapolation, 5 rates, 6 integration, 7 advect_pos, 8 post-step, 9 other) and clears. */
+ * extrapolation, 5 rates, 6 integration, 7 advect_pos, 8 post-step, 9 other, 10 neighbour
+ * lists) and clears. */
 int tsg_profile(int enable);
 int tsg_profile_read(double* ms, int64_t* counts, int nphase);
 

@@ -16,7 +16,7 @@ TSG_ADVECT_FULL, TSG_ADVECT_LF_HALF, TSG_ADVECT_POS, TSG_ADVECT_SOMETHING, TSG_E
     TSG_RK_INIT, TSG_RK_STAGE, TSG_RK_FINAL = range(1, 9)
 TSG_ERR_CELL_OOB, TSG_ERR_NONFINITE, TSG_ERR_PACK_RANGE = 1, 2, 4
 PHASES = ("sort", "kernel_corr", "init_tmp", "eos_adapt", "boundary", "rates", "integrate", "advect_pos",
-          "post", "other")
+          "post", "other", "neighbour_lists")
 
 
 class tsg_config(ctypes.Structure):

@@ -111,13 +111,11 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
                                                const int* __restrict__ dstart, const int* __restrict__ sstart,
                                                bool flow_i, F&& body) {
     const float4 hi_i = HI[i], lo_i = LO[i], pf_i = PF[i];
-    long long cc[3];
-    for (int d = 0; d < 3; ++d) {
-        double t = ((double)(d == 0 ? hi_i.x : d == 1 ? hi_i.y : hi_i.z) +
-                    (double)(d == 0 ? lo_i.x : d == 1 ? lo_i.y : lo_i.z)) / k.grid;
-        if (!(fabs(t) < 2147483647.0)) return;
-        cc[d] = (int)t;
-    }
+    const double tx = ((double)hi_i.x + (double)lo_i.x) / k.grid;
+    const double ty = ((double)hi_i.y + (double)lo_i.y) / k.grid;
+    const double tz = ((double)hi_i.z + (double)lo_i.z) / k.grid;
+    if (!(fabs(tx) < 2147483647.0 && fabs(ty) < 2147483647.0 && fabs(tz) < 2147483647.0)) return;
+    const long long cc0 = (int)tx, cc1 = (int)ty, cc2 = (int)tz;
     const bool pf = fabsf(pf_i.x) < k.pf_lim && fabsf(pf_i.y) < k.pf_lim && fabsf(pf_i.z) < k.pf_lim;
     const long long ny = k.gnum[1], nz = k.gnum[2], G = k.G;
     for (int blk = 0; blk < (flow_i ? 2 : 1); ++blk) {
@@ -126,7 +124,7 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
         for (int ox = -1; ox <= 1; ++ox) {
 #pragma unroll 1
             for (int oy = (DIM == 3 ? -1 : 0); oy <= (DIM == 3 ? 1 : 0); ++oy) {
-                long long f0 = (cc[0] + ox) * ny * nz + (cc[1] + oy) * nz + cc[2];
+                long long f0 = (cc0 + ox) * ny * nz + (cc1 + oy) * nz + cc2;
                 long long lo = f0 - 1 > 0 ? f0 - 1 : 0;
                 long long hi = f0 + 1 < G - 1 ? f0 + 1 : G - 1;
                 if (lo > hi) continue;
@@ -273,6 +271,127 @@ __global__ void k_lists(K32 k, const float4* __restrict__ HI, const float4* __re
         ++m;
     });
     cnt[i] = m;
+}
+
+// Warp-per-cell list build (3D): the lanes of a warp are the particles of one cell, so
+// they share one stencil; each candidate row is staged through shared memory with
+// coalesced loads and tested by every lane from a broadcast read.  Lanes whose particle
+// sits in an aliased cell (true cell coordinates outside the grid) and particles in the
+// out-of-grid bin take the per-particle path.
+template <int DIM>
+__global__ void k_lists_cell(K32 k, int self_blk, const float4* __restrict__ HI,
+                                                    const float4* __restrict__ LO, const float4* __restrict__ PF,
+                                                    const int* __restrict__ dstart, const int* __restrict__ sstart,
+                                                    int* __restrict__ cnt, int* __restrict__ nbr) {
+    __shared__ float4 sh_hi[4][32];
+    __shared__ float4 sh_lo[4][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const long long c = (long long)blockIdx.x * 4 + wib;
+    if (c >= k.G) return;
+    const int* own = self_blk == 0 ? dstart : sstart;
+    const int cb = own[c], ce = own[c + 1];
+    if (cb >= ce) return;
+    const long long ny = k.gnum[1], nz = k.gnum[2], G = k.G;
+    const long long cx = c / (ny * nz), cy = (c / nz) % ny, cz = c % nz;
+    for (int p0 = cb; p0 < ce; p0 += 32) {
+        const int i = p0 + lane;
+        const bool active = i < ce;
+        float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
+        bool flow_i = false, alias = false;
+        if (active) {
+            hi_i = HI[i];
+            lo_i = LO[i];
+            flow_i = is_flow(tf_type(lo_i.w));
+            const double tx = ((double)hi_i.x + (double)lo_i.x) / k.grid;
+            const double ty = ((double)hi_i.y + (double)lo_i.y) / k.grid;
+            const double tz = ((double)hi_i.z + (double)lo_i.z) / k.grid;
+            alias = !(fabs(tx) < 2147483647.0 && fabs(ty) < 2147483647.0 && fabs(tz) < 2147483647.0) ||
+                    (long long)(int)tx != cx || (long long)(int)ty != cy || (long long)(int)tz != cz;
+        }
+        int m = 0;
+        const bool any_flow = __any_sync(0xffffffffu, active && flow_i && !alias);
+        for (int blk = 0; blk < (any_flow ? 2 : 1); ++blk) {
+            const int* cs = blk == 0 ? dstart : sstart;
+#pragma unroll 1
+            for (int ox = -1; ox <= 1; ++ox) {
+#pragma unroll 1
+                for (int oy = (DIM == 3 ? -1 : 0); oy <= (DIM == 3 ? 1 : 0); ++oy) {
+                    const long long f0 = (cx + ox) * ny * nz + (cy + oy) * nz + cz;
+                    const long long lo = f0 - 1 > 0 ? f0 - 1 : 0;
+                    const long long hi = f0 + 1 < G - 1 ? f0 + 1 : G - 1;
+                    if (lo > hi) continue;
+                    const int rb = cs[lo], re = cs[hi + 1];
+                    for (int base = rb; base < re; base += 32) {
+                        const int jj = base + lane;
+                        if (jj < re) {
+                            sh_hi[wib][lane] = HI[jj];
+                            sh_lo[wib][lane] = LO[jj];
+                        }
+                        __syncwarp();
+                        const int mm = re - base < 32 ? re - base : 32;
+                        if (active && !alias && (blk == 0 || flow_i)) {
+#pragma unroll 4
+                            for (int t = 0; t < mm; ++t) {
+                                const float4 hj = sh_hi[wib][t], lj = sh_lo[wib][t];
+                                const int j = base + t;
+                                if (j == i) continue;
+                                if (!flow_i && !is_flow(tf_type(lj.w))) continue;
+                                const float dx = (hi_i.x - hj.x) + (lo_i.x - lj.x);
+                                const float dy = (hi_i.y - hj.y) + (lo_i.y - lj.y);
+                                float r2 = dx * dx + dy * dy;
+                                if (DIM == 3) {
+                                    const float dz = (hi_i.z - hj.z) + (lo_i.z - lj.z);
+                                    r2 += dz * dz;
+                                }
+                                if (r2 < k.R2) {
+                                    if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
+                                    ++m;
+                                }
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
+            }
+        }
+        if (active) cnt[i] = alias ? -1 : m;  // -1: rebuilt by k_lists_fixup
+    }
+}
+
+// Per-particle list build for particles the warp-per-cell pass could not serve (their true
+// cell differs from the storage cell); flagged with count -1.
+template <int DIM>
+__global__ void k_lists_fixup(K32 k, const float4* __restrict__ HI, const float4* __restrict__ LO,
+                              const float4* __restrict__ PF, const int* __restrict__ dstart,
+                              const int* __restrict__ sstart, int* __restrict__ cnt, int* __restrict__ nbr) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.n; i += gridDim.x * blockDim.x) {
+        if (cnt[i] >= 0) continue;
+        const bool flow_i = is_flow(tf_type(PF[i].w));
+        int m = 0;
+        enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float*, float) {
+            if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
+            ++m;
+        });
+        cnt[i] = m;
+    }
+}
+
+// Per-particle list build for an index range (out-of-grid bin).
+template <int DIM>
+__global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float4* __restrict__ HI,
+                              const float4* __restrict__ LO, const float4* __restrict__ PF,
+                              const int* __restrict__ dstart, const int* __restrict__ sstart,
+                              int* __restrict__ cnt, int* __restrict__ nbr) {
+    const int b0 = bounds[0], b1 = bounds[1];
+    for (int i = b0 + blockIdx.x * blockDim.x + threadIdx.x; i < b1; i += gridDim.x * blockDim.x) {
+        const bool flow_i = is_flow(tf_type(PF[i].w));
+        int m = 0;
+        enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float*, float) {
+            if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
+            ++m;
+        });
+        cnt[i] = m;
+    }
 }
 
 // ---------------------------------------------------------------- transient state
@@ -769,6 +888,26 @@ __global__ void k_nbr_fill32(K32 k, const float4* HI, const float4* LO, const fl
                         [&](int j, const float*, float) { list[m++] = j; });
 }
 
+__global__ void k_nbr_count_ell(K32 k, const int* cnt, int* counts) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < k.n) counts[i] = cnt[i];
+}
+
+template <int DIM>
+__global__ void k_nbr_fill_ell(K32 k, const float4* HI, const float4* LO, const float4* PF, const int* ds,
+                               const int* ss, const int* cnt, const int* nbr, const int* off, int* list) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    const int m = cnt[i];
+    if (m <= k.maxn) {
+        for (int q = 0; q < m; ++q) list[off[i] + q] = nbr[(size_t)q * k.n + i];
+    } else {
+        int w = off[i];
+        enum_neighbors<DIM>(k, i, HI, LO, PF, ds, ss, is_flow(tf_type(PF[i].w)),
+                            [&](int j, const float*, float) { list[w++] = j; });
+    }
+}
+
 }  // namespace
 
 // ====================================================================== host side
@@ -971,16 +1110,34 @@ void fp32_destroy(Fp32State* st) {
 }
 
 void fp32_sort(Fp32State& st, cudaStream_t s) {
-    PhaseScope ph(s, PH_SORT);
-    if (st.nd > 0) {
-        build_cells(st, 0, st.nd, st.dcount, st.dstart, s, true);
-        st.cur = 1 - st.cur;
-    } else {
-        cudaMemsetAsync(st.dstart, 0, sizeof(int) * (st.k.G + 2), s);
+    {
+        PhaseScope ph(s, PH_SORT);
+        if (st.nd > 0) {
+            build_cells(st, 0, st.nd, st.dcount, st.dstart, s, true);
+            st.cur = 1 - st.cur;
+        } else {
+            cudaMemsetAsync(st.dstart, 0, sizeof(int) * (st.k.G + 2), s);
+        }
     }
     const K32& k = st.k;
     P32& p = st.P[st.cur];
-    DISPATCH32(k, k_lists, nblk(k.n), k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr);
+    {
+        PhaseScope ph2(s, PH_LISTS);
+        if (k.dim == 3) {
+            const int nb = (int)((k.G + 3) / 4);
+            TSG_LAUNCH(k_lists_cell<3>, nb, 128, s, k, 0, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr);
+            TSG_LAUNCH(k_lists_cell<3>, nb, 128, s, k, 1, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr);
+            // particles in the out-of-grid bins (bounds read on the device)
+            TSG_LAUNCH(k_lists_range<3>, 64, TPB, s, k, st.dstart + k.G, p.hi, p.lo, st.pf, st.dstart,
+                       st.sstart, st.T.cnt, st.T.nbr);
+            TSG_LAUNCH(k_lists_range<3>, 64, TPB, s, k, st.sstart + k.G, p.hi, p.lo, st.pf, st.dstart,
+                       st.sstart, st.T.cnt, st.T.nbr);
+            TSG_LAUNCH(k_lists_fixup<3>, 2 * 152, TPB, s, k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt,
+                       st.T.nbr);
+        } else {
+            DISPATCH32(k, k_lists, nblk(k.n), k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr);
+        }
+    }
     st.lists_valid = true;
 }
 
@@ -1070,6 +1227,12 @@ const int* fp32_cell_start(const Fp32State& st) { return st.dstart; }
 void fp32_neighbors(Fp32State& st, int* counts, int* offsets, int* list, cudaStream_t s) {
     const K32& k = st.k;
     P32& p = st.P[st.cur];
+    if (st.lists_valid) {  // report the lists the physics kernels use
+        if (!list) TSG_LAUNCH(k_nbr_count_ell, nblk(k.n), TPB, s, k, st.T.cnt, counts);
+        else DISPATCH32(k, k_nbr_fill_ell, nblk(k.n), k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt,
+                        st.T.nbr, offsets, list);
+        return;
+    }
     if (!list) DISPATCH32(k, k_nbr_count32, nblk(k.n), k, p.hi, p.lo, st.pf, st.dstart, st.sstart, counts);
     else DISPATCH32(k, k_nbr_fill32, nblk(k.n), k, p.hi, p.lo, st.pf, st.dstart, st.sstart, offsets, list);
 }

@@ -17,7 +17,7 @@ void note_launch();
 
 // Phase profiling: when enabled, every launcher brackets its kernels with CUDA events
 // recorded on the launching stream, and elapsed times are summed per phase.
-enum Phase { PH_SORT = 0, PH_CORR, PH_INIT, PH_PRE, PH_BDY, PH_RATES, PH_INTEGRATE, PH_POS, PH_POST, PH_OTHER, PH_COUNT };
+enum Phase { PH_SORT = 0, PH_CORR, PH_INIT, PH_PRE, PH_BDY, PH_RATES, PH_INTEGRATE, PH_POS, PH_POST, PH_OTHER, PH_LISTS, PH_COUNT };
 struct PhaseScope {
     PhaseScope(cudaStream_t s, int phase);
     ~PhaseScope();
