@@ -64,7 +64,9 @@ def test_neighbor_sets_match(oracle_lib, native, scene):
     mismatched = 0
     for oi in range(oid.size):
         gk = g_of_id[int(oid[oi])]
-        gset = set(gid[gl[goff[gk]:goff[gk + 1]]].tolist())
+        glist = gid[gl[goff[gk]:goff[gk + 1]]].tolist()
+        gset = set(glist)
+        assert len(gset) == len(glist), f"duplicate list entries for particle {oid[oi]}"
         oset = set(oid[ol[ooff[oi]:ooff[oi + 1]]].tolist())
         if mt[oi] not in (1, 2):
             oset &= flow_ids  # boundary particles list flow neighbours only

@@ -45,7 +45,7 @@ struct K32 {
     int gnum[3];
     long long G;
     double vs[3], grid;
-    float Q, h1, kk, kk6, wgrad, cub1, cub2, R2, R2lo, R2hi, pf_lim;
+    float Q, inv_grid, h1, kk, kk6, wgrad, cub1, cub2, R2, R2lo, R2hi, pf_lim;
     float visc_fac, eps_h2, rho0, B, gamma, dt, hdt, g[3], rep_fac, diam, h075, r_eps;
     float ds[3], de[3];
 };
@@ -67,6 +67,17 @@ struct CSum {
     }
     __device__ __forceinline__ float get() { flush(); return s; }
 };
+
+// Cell coordinate trunc((hi + lo) / grid) with the f64 semantics of the reference's cast:
+// an f32 estimate decides unless it lies within 1e-3 of an integer, where f64 decides.
+__device__ __forceinline__ long long cell_coord(const K32& k, float hi, float lo, bool& ok) {
+    const float tf = (hi + lo) * k.inv_grid;
+    const float fr = tf - truncf(tf);
+    if (fabsf(tf) < 1.0e6f && fabsf(fr) > 1e-3f && fabsf(fr) < 0.999f) return (long long)(int)tf;
+    const double t = ((double)hi + (double)lo) / k.grid;
+    if (!(fabs(t) < 2147483647.0)) { ok = false; return 0; }
+    return (long long)(int)t;
+}
 
 // Kernel value and gradient factor: W(r) and G with grad W = G * dx.
 __device__ __forceinline__ float w_val(const K32& k, float r) {
@@ -111,11 +122,11 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
                                                const int* __restrict__ dstart, const int* __restrict__ sstart,
                                                bool flow_i, F&& body) {
     const float4 hi_i = HI[i], lo_i = LO[i], pf_i = PF[i];
-    const double tx = ((double)hi_i.x + (double)lo_i.x) / k.grid;
-    const double ty = ((double)hi_i.y + (double)lo_i.y) / k.grid;
-    const double tz = ((double)hi_i.z + (double)lo_i.z) / k.grid;
-    if (!(fabs(tx) < 2147483647.0 && fabs(ty) < 2147483647.0 && fabs(tz) < 2147483647.0)) return;
-    const long long cc0 = (int)tx, cc1 = (int)ty, cc2 = (int)tz;
+    bool ok = true;
+    const long long cc0 = cell_coord(k, hi_i.x, lo_i.x, ok);
+    const long long cc1 = cell_coord(k, hi_i.y, lo_i.y, ok);
+    const long long cc2 = cell_coord(k, hi_i.z, lo_i.z, ok);
+    if (!ok) return;
     const bool pf = fabsf(pf_i.x) < k.pf_lim && fabsf(pf_i.y) < k.pf_lim && fabsf(pf_i.z) < k.pf_lim;
     const long long ny = k.gnum[1], nz = k.gnum[2], G = k.G;
     for (int blk = 0; blk < (flow_i ? 2 : 1); ++blk) {
@@ -153,18 +164,21 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
     }
 }
 
-// Iterate i's neighbour list (or traverse when it overflowed).
-template <int DIM, class F>
-__device__ __forceinline__ void for_list(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
+// Iterate i's neighbour list (FB = false) or traverse its stencil directly (FB = true: the
+// particle's list overflowed).  The next list index is fetched one iteration ahead.
+template <int DIM, bool FB, class F>
+__device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
                                          const float4* __restrict__ HI, const float4* __restrict__ LO,
                                          const float4* __restrict__ PF, const int* __restrict__ dstart,
                                          const int* __restrict__ sstart, bool flow_i, F&& body) {
-    const int m = cnt[i];
-    if (m <= k.maxn) {
+    if (!FB) {
+        const int m = cnt[i];
         const float4 hi_i = HI[i], lo_i = LO[i];
+        int jn = m > 0 ? nbr[i] : 0;
 #pragma unroll 2
         for (int s = 0; s < m; ++s) {
-            const int j = nbr[(size_t)s * k.n + i];
+            const int j = jn;
+            if (s + 1 < m) jn = nbr[(size_t)(s + 1) * k.n + i];
             float d[3];
             delta<DIM>(hi_i, lo_i, HI[j], LO[j], d);
             float r2 = d[0] * d[0] + d[1] * d[1];
@@ -178,6 +192,26 @@ __device__ __forceinline__ void for_list(const K32& k, int i, const int* __restr
     }
 }
 
+// Particle loop shared by the list kernels (FB = false: one particle per thread, skipping
+// overflowed lists) and their overflow passes (FB = true: grid-stride over the overflow list).
+struct Ovf {
+    const int* list;
+    const int* count;
+};
+#define FOR_PARTICLES(FB, BASE, N, OVF, CNT, MAXN, ...)                                         \
+    do {                                                                                        \
+        if (!(FB)) {                                                                            \
+            const int i = (BASE) + blockIdx.x * blockDim.x + threadIdx.x;                       \
+            if (i < (N) && (CNT)[i] <= (MAXN)) { __VA_ARGS__ }                                  \
+        } else {                                                                                \
+            const int no = *(OVF).count;                                                        \
+            for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < no; q += gridDim.x * blockDim.x) { \
+                const int i = (OVF).list[q];                                                    \
+                if (i >= (BASE) && i < (N)) { __VA_ARGS__ }                                     \
+            }                                                                                   \
+        }                                                                                       \
+    } while (0)
+
 // ---------------------------------------------------------------- sort (dynamic block)
 __global__ void k_hash32(K32 k, int count_n, int base, const float4* __restrict__ HI, const float4* __restrict__ LO,
                          int* __restrict__ cell_of, int* __restrict__ rank, int* __restrict__ count, int* __restrict__ err) {
@@ -188,11 +222,8 @@ __global__ void k_hash32(K32 k, int count_n, int base, const float4* __restrict_
     long long idx[3];
     bool ok = true;
     const float hv[3] = {h.x, h.y, h.z}, lv[3] = {l.x, l.y, l.z};
-    for (int d = 0; d < 3; ++d) {
-        double v = ((double)hv[d] + (double)lv[d]) / k.grid;
-        if (!(fabs(v) < 2147483647.0)) { ok = false; idx[d] = 0; }
-        else idx[d] = (int)v;
-    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) idx[d] = cell_coord(k, hv[d], lv[d], ok);
     long long f = idx[0] * k.gnum[1] * k.gnum[2] + idx[1] * k.gnum[2] + idx[2];
     if (!ok || f < 0 || f >= k.G) {
         f = k.G;
@@ -257,11 +288,16 @@ __global__ void k_reorder32(K32 k, int count_n, int base, const int* __restrict_
     PF[dst] = make_float4(pfv[0], pfv[1], pfv[2], l.w);
 }
 
+// Record a particle whose neighbours exceed the list capacity (processed by FB passes).
+__device__ __forceinline__ void note_overflow(int* ovf_list, int* novf, int i) {
+    ovf_list[atomicAdd(novf, 1)] = i;
+}
+
 // ---------------------------------------------------------------- neighbour lists
 template <int DIM>
 __global__ void k_lists(K32 k, const float4* __restrict__ HI, const float4* __restrict__ LO,
                         const float4* __restrict__ PF, const int* __restrict__ dstart, const int* __restrict__ sstart,
-                        int* __restrict__ cnt, int* __restrict__ nbr) {
+                        int* __restrict__ cnt, int* __restrict__ nbr, int* __restrict__ ovf_list, int* __restrict__ novf) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     const bool flow_i = is_flow(tf_type(PF[i].w));
@@ -271,6 +307,7 @@ __global__ void k_lists(K32 k, const float4* __restrict__ HI, const float4* __re
         ++m;
     });
     cnt[i] = m;
+    if (m > k.maxn) note_overflow(ovf_list, novf, i);
 }
 
 // Warp-per-cell list build (3D): the lanes of a warp are the particles of one cell, so
@@ -279,19 +316,20 @@ __global__ void k_lists(K32 k, const float4* __restrict__ HI, const float4* __re
 // sits in an aliased cell (true cell coordinates outside the grid) and particles in the
 // out-of-grid bin take the per-particle path.
 template <int DIM>
-__global__ void k_lists_cell(K32 k, int self_blk, const float4* __restrict__ HI,
-                                                    const float4* __restrict__ LO, const float4* __restrict__ PF,
-                                                    const int* __restrict__ dstart, const int* __restrict__ sstart,
-                                                    int* __restrict__ cnt, int* __restrict__ nbr) {
+__global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells, const int* __restrict__ cell_count,
+                             const float4* __restrict__ HI, const float4* __restrict__ LO,
+                             const float4* __restrict__ PF, const int* __restrict__ dstart,
+                             const int* __restrict__ sstart, int* __restrict__ cnt, int* __restrict__ nbr,
+                             int* __restrict__ ovf_list, int* __restrict__ novf) {
     __shared__ float4 sh_hi[4][32];
     __shared__ float4 sh_lo[4][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const long long c = (long long)blockIdx.x * 4 + wib;
-    if (c >= k.G) return;
     const int* own = self_blk == 0 ? dstart : sstart;
-    const int cb = own[c], ce = own[c + 1];
-    if (cb >= ce) return;
+    const int ncell = *cell_count;
     const long long ny = k.gnum[1], nz = k.gnum[2], G = k.G;
+    for (int w = blockIdx.x * 4 + wib; w < ncell; w += gridDim.x * 4) {
+    const long long c = cells[w];
+    const int cb = own[c], ce = own[c + 1];
     const long long cx = c / (ny * nz), cy = (c / nz) % ny, cz = c % nz;
     for (int p0 = cb; p0 < ce; p0 += 32) {
         const int i = p0 + lane;
@@ -302,11 +340,9 @@ __global__ void k_lists_cell(K32 k, int self_blk, const float4* __restrict__ HI,
             hi_i = HI[i];
             lo_i = LO[i];
             flow_i = is_flow(tf_type(lo_i.w));
-            const double tx = ((double)hi_i.x + (double)lo_i.x) / k.grid;
-            const double ty = ((double)hi_i.y + (double)lo_i.y) / k.grid;
-            const double tz = ((double)hi_i.z + (double)lo_i.z) / k.grid;
-            alias = !(fabs(tx) < 2147483647.0 && fabs(ty) < 2147483647.0 && fabs(tz) < 2147483647.0) ||
-                    (long long)(int)tx != cx || (long long)(int)ty != cy || (long long)(int)tz != cz;
+            bool ok = true;
+            alias = cell_coord(k, hi_i.x, lo_i.x, ok) != cx || cell_coord(k, hi_i.y, lo_i.y, ok) != cy ||
+                    cell_coord(k, hi_i.z, lo_i.z, ok) != cz || !ok;
         }
         int m = 0;
         const bool any_flow = __any_sync(0xffffffffu, active && flow_i && !alias);
@@ -354,8 +390,26 @@ __global__ void k_lists_cell(K32 k, int self_blk, const float4* __restrict__ HI,
                 }
             }
         }
-        if (active) cnt[i] = alias ? -1 : m;  // -1: rebuilt by k_lists_fixup
+        if (active) {
+            cnt[i] = alias ? -1 : m;  // -1: rebuilt by k_lists_fixup
+            if (!alias && m > k.maxn) note_overflow(ovf_list, novf, i);
+        }
     }
+    }
+}
+
+// Non-empty cells of one block's cell table (order irrelevant: each cell is independent).
+__global__ void k_nonempty_cells(long long G, const int* __restrict__ start, int* __restrict__ cells,
+                                 int* __restrict__ count) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool pred = c < G && start[c + 1] > start[c];
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pred) cells[base + __popc(mask & ((1u << lane) - 1u))] = (int)c;
 }
 
 // Per-particle list build for particles the warp-per-cell pass could not serve (their true
@@ -363,7 +417,8 @@ __global__ void k_lists_cell(K32 k, int self_blk, const float4* __restrict__ HI,
 template <int DIM>
 __global__ void k_lists_fixup(K32 k, const float4* __restrict__ HI, const float4* __restrict__ LO,
                               const float4* __restrict__ PF, const int* __restrict__ dstart,
-                              const int* __restrict__ sstart, int* __restrict__ cnt, int* __restrict__ nbr) {
+                              const int* __restrict__ sstart, int* __restrict__ cnt, int* __restrict__ nbr,
+                              int* __restrict__ ovf_list, int* __restrict__ novf) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.n; i += gridDim.x * blockDim.x) {
         if (cnt[i] >= 0) continue;
         const bool flow_i = is_flow(tf_type(PF[i].w));
@@ -373,6 +428,7 @@ __global__ void k_lists_fixup(K32 k, const float4* __restrict__ HI, const float4
             ++m;
         });
         cnt[i] = m;
+        if (m > k.maxn) note_overflow(ovf_list, novf, i);
     }
 }
 
@@ -381,7 +437,8 @@ template <int DIM>
 __global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float4* __restrict__ HI,
                               const float4* __restrict__ LO, const float4* __restrict__ PF,
                               const int* __restrict__ dstart, const int* __restrict__ sstart,
-                              int* __restrict__ cnt, int* __restrict__ nbr) {
+                              int* __restrict__ cnt, int* __restrict__ nbr, int* __restrict__ ovf_list,
+                              int* __restrict__ novf) {
     const int b0 = bounds[0], b1 = bounds[1];
     for (int i = b0 + blockIdx.x * blockDim.x + threadIdx.x; i < b1; i += gridDim.x * blockDim.x) {
         const bool flow_i = is_flow(tf_type(PF[i].w));
@@ -391,6 +448,7 @@ __global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float
             ++m;
         });
         cnt[i] = m;
+        if (m > k.maxn) note_overflow(ovf_list, novf, i);
     }
 }
 
@@ -432,37 +490,37 @@ __device__ __forceinline__ void inv_store(const K32& k, float* L, int i, const d
     for (int q = 0; q < 9; ++q) L[(size_t)q * k.n + i] = (float)inv[q];
 }
 
-// CSPM (eng/solver_sph_base.py:386-423) + init_real2tmp (eng/solver_sph_base.py:67-74).
-template <int DIM>
+// CSPM (eng/solver_sph_base.py:386-423).
+template <int DIM, bool FB>
 __global__ void k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
-                         const int* __restrict__ sstart) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) return;
-    const int ti = tf_type(p.lo[i].w);
-    const bool flow_i = is_flow(ti);
-    const bool want_L = k.corr == 1 && flow_i;
-    CSum s;
-    float L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for_list<DIM>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, flow_i,
-                  [&](int j, const float* d, float r2, int sidx) {
-        const float4 hj = p.hi[j];
-        const int tj = tf_type(p.lo[j].w);
-        const float r = sqrtf(r2);
-        if (is_flow(tj)) s.add(hj.w * w_val(k, r));
-        if ((sidx & 7) == 7) s.flush();
-        if (want_L && tj == ti) {
-            const float gf = w_grad(k, r) * hj.w;
-            for (int a = 0; a < DIM; ++a)
-                for (int b = 0; b < DIM; ++b) L[3 * a + b] += (-d[a]) * (gf * d[b]);
+                         const int* __restrict__ sstart, Ovf ovf) {
+    FOR_PARTICLES(FB, 0, k.n, ovf, t.cnt, k.maxn, {
+        const int ti = tf_type(p.lo[i].w);
+        const bool flow_i = is_flow(ti);
+        const bool want_L = k.corr == 1 && flow_i;
+        CSum s;
+        float L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, flow_i,
+                          [&](int j, const float* d, float r2, int sidx) {
+            const float4 hj = p.hi[j];
+            const int tj = tf_type(p.lo[j].w);
+            const float r = sqrtf(r2);
+            if (is_flow(tj)) s.add(hj.w * w_val(k, r));
+            if ((sidx & 7) == 7) s.flush();
+            if (want_L && tj == ti) {
+                const float gf = w_grad(k, r) * hj.w;
+                for (int a = 0; a < DIM; ++a)
+                    for (int b = 0; b < DIM; ++b) L[3 * a + b] += (-d[a]) * (gf * d[b]);
+            }
+        });
+        const float sum = s.get();
+        t.cf[i] = sum != 0.f ? 1.f / sum : 1.f;
+        if (k.corr == 1) {
+            double m[9];
+            for (int q = 0; q < 9; ++q) m[q] = L[q];
+            inv_store<DIM>(k, t.L, i, m, want_L);
         }
     });
-    const float sum = s.get();
-    t.cf[i] = sum != 0.f ? 1.f / sum : 1.f;
-    if (k.corr == 1) {
-        double m[9];
-        for (int q = 0; q < 9; ++q) m[q] = L[q];
-        inv_store<DIM>(k, t.L, i, m, want_L);
-    }
 }
 
 __global__ void k_init_tmp32(K32 k, P32 p, T32 t) {
@@ -503,108 +561,102 @@ __global__ void k_pre32(K32 k, P32 p, T32 t) {
     t.pr[i] = make_float2(pr, rt);
 }
 
-// Boundary extrapolation for dummy / repulsive / rigid particles (WC).
-template <int DIM>
+// Boundary extrapolation for dummy / repulsive / rigid particles in [base, base + count_n) (WC).
+template <int DIM, bool FB>
 __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
-                        const int* __restrict__ sstart, int base, int count_n) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= count_n) return;
-    const int i = base + q;
-    const int ti = tf_type(p.lo[i].w);
-    if (!(ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID)) return;
-    CSum bv[3], bp;
-    const float4 hi_i = p.hi[i], lo_i = p.lo[i];
-    const float yi_hi = hi_i.y, yi_lo = lo_i.y;
-    for_list<DIM>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
-                  [&](int j, const float* d, float r2, int sidx) {
-        const float w = w_val(k, sqrtf(r2));
-        const float mV = p.hi[j].w;
-        const float4 vt = t.vt[j];
-        const float2 pr = t.pr[j];
-        const float mw = mV * w;
-        bv[0].add(mw * vt.x);
-        bv[1].add(mw * vt.y);
-        if (DIM == 3) bv[2].add(mw * vt.z);
-        const float dy = (yi_hi - p.hi[j].y) + (yi_lo - p.lo[j].y);
-        bp.add(mw * (pr.x + pr.y * k.g[1] * dy));
-        if ((sidx & 7) == 7) { bv[0].flush(); bv[1].flush(); bv[2].flush(); bp.flush(); }
+                        const int* __restrict__ sstart, int base, int count_n, Ovf ovf) {
+    const int lim = base + count_n;
+    FOR_PARTICLES(FB, base, lim, ovf, t.cnt, k.maxn, {
+        const int ti = tf_type(p.lo[i].w);
+        if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
+            CSum bv[3], bp;
+            const float4 hi_i = p.hi[i], lo_i = p.lo[i];
+            for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
+                              [&](int j, const float* d, float r2, int sidx) {
+                const float w = w_val(k, sqrtf(r2));
+                const float mV = p.hi[j].w;
+                const float4 vt = t.vt[j];
+                const float2 pr = t.pr[j];
+                const float mw = mV * w;
+                bv[0].add(mw * vt.x);
+                bv[1].add(mw * vt.y);
+                if (DIM == 3) bv[2].add(mw * vt.z);
+                bp.add(mw * (pr.x + pr.y * k.g[1] * d[1]));
+                if ((sidx & 7) == 7) { bv[0].flush(); bv[1].flush(); bv[2].flush(); bp.flush(); }
+            });
+            (void)hi_i; (void)lo_i;
+            const float f = t.cf[i];
+            const float4 v = p.vel[i];
+            const float pv = fmaxf(bp.get() * f, 0.f);
+            const float b0 = bv[0].get(), b1 = bv[1].get(), b2 = DIM == 3 ? bv[2].get() : 0.f;
+            t.vt[i] = make_float4(2.f * v.x - b0 * f, 2.f * v.y - b1 * f, 2.f * v.z - b2 * f, pv / (k.rho0 * k.rho0));
+            t.pr[i] = make_float2(pv, k.rho0);
+            t.drt[i] = 0.f;
+            p.vel[i].w = pv;
+            if (ti == MAT_RIGID) { t.dd[i] = 0.f; t.dv[i] = make_float4(0.f, 0.f, 0.f, 0.f); }
+        }
     });
-    const float f = t.cf[i];
-    const float4 v = p.vel[i];
-    const float pv = fmaxf(bp.get() * f, 0.f);
-    const float b0 = bv[0].get(), b1 = bv[1].get(), b2 = DIM == 3 ? bv[2].get() : 0.f;
-    t.vt[i] = make_float4(2.f * v.x - b0 * f, 2.f * v.y - b1 * f, 2.f * v.z - b2 * f, pv / (k.rho0 * k.rho0));
-    t.pr[i] = make_float2(pv, k.rho0);
-    t.drt[i] = 0.f;
-    p.vel[i].w = pv;
-    if (ti == MAT_RIGID) { t.dd[i] = 0.f; t.dv[i] = make_float4(0.f, 0.f, 0.f, 0.f); }
-}
-
-template <int DIM>
-__device__ __forceinline__ void rep_acc(const K32& k, const float* d, float r2, float* acc) {
-    const float rn = sqrtf(r2);
-    const float chi = (rn > 0.f && rn < k.diam) ? 1.f - rn / k.diam : 0.f;
-    const float gm = rn / k.h075;
-    float f = 0.f;
-    if (gm > 0.f && gm <= 2.f / 3.f) f = 2.f / 3.f;
-    else if (gm > 2.f / 3.f && gm <= 1.f) f = 2.f * gm - 1.5f * gm * gm;
-    else if (gm > 1.f && gm < 2.f) f = 0.5f * (2.f - gm) * (2.f - gm);
-    const float s = k.rep_fac * chi * f / r2;
-    for (int a = 0; a < DIM; ++a) acc[a] += s * d[a];
 }
 
 // WCSPH continuity + momentum (eng/solver_sph_wc.py:108-126).
-template <int DIM>
+template <int DIM, bool FB, bool CORR>
 __global__ void k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
-                          const int* __restrict__ sstart) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.nd) return;
-    if (tf_type(p.lo[i].w) != MAT_FLUID) return;
-    const float4 vti = t.vt[i];
-    const float rti = k.rho0 + t.drt[i];
-    const float visc_b = k.rho0 / rti;
-    float L[9];
-    if (k.corr == 1)
-        for (int q = 0; q < 9; ++q) L[q] = t.L[(size_t)q * k.n + i];
-    CSum dd, dv[3];
-    float rep[3] = {0.f, 0.f, 0.f};
-    const bool rep_on = k.boundary == 3 || k.boundary == 4;
-    for_list<DIM>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
-                  [&](int j, const float* d, float r2, int sidx) {
-        const float4 hj = p.hi[j];
-        const int tj = tf_type(p.lo[j].w);
-        const float4 vtj = t.vt[j];
-        const float r = sqrtf(r2);
-        const float gf = w_grad(k, r);
-        const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = vti.z - vtj.z;
-        // continuity: m_Vj (v_i - v_j) . (L_i grad W)
-        float gx = gf * d[0], gy = gf * d[1], gz = DIM == 3 ? gf * d[2] : 0.f;
-        if (k.corr == 1) {
-            float cx = L[0] * gx + L[1] * gy + (DIM == 3 ? L[2] * gz : 0.f);
-            float cy = L[3] * gx + L[4] * gy + (DIM == 3 ? L[5] * gz : 0.f);
-            float cz = DIM == 3 ? L[6] * gx + L[7] * gy + L[8] * gz : 0.f;
-            dd.add(hj.w * (dvx * cx + dvy * cy + (DIM == 3 ? dvz * cz : 0.f)));
-        } else {
-            dd.add(hj.w * (dvx * gx + dvy * gy + (DIM == 3 ? dvz * gz : 0.f)));
-        }
-        // viscosity (fluid or boundary neighbours) and pressure, on the uncorrected gradient
-        const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
-        float cv = 0.f;
-        if (tj == MAT_FLUID || tj == MAT_DUMMY || tj == MAT_REP || tj == MAT_RIGID) {
-            cv = k.visc_fac * hj.w * fminf(vdx, 0.f) / (r2 + k.eps_h2);
-            if (tj != MAT_FLUID) cv *= visc_b;
-        }
-        const float cp = -k.rho0 * hj.w * (vti.w + vtj.w);
-        const float sc = (cv + cp) * gf;
-        dv[0].add(sc * d[0]);
-        dv[1].add(sc * d[1]);
-        if (DIM == 3) dv[2].add(sc * d[2]);
-        if (rep_on && tj == MAT_REP) rep_acc<DIM>(k, d, r2, rep);
-        if ((sidx & 7) == 7) { dd.flush(); dv[0].flush(); dv[1].flush(); dv[2].flush(); }
+                          const int* __restrict__ sstart, Ovf ovf) {
+    FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
+      if (tf_type(p.lo[i].w) == MAT_FLUID) {
+        const float4 vti = t.vt[i];
+        const float rti = k.rho0 + t.drt[i];
+        const float visc_b = k.rho0 / rti;
+        float L[9];
+        if (CORR)
+            for (int q = 0; q < 9; ++q) L[q] = t.L[(size_t)q * k.n + i];
+        CSum dd, dv[3];
+        const bool rep_on = k.boundary == 3 || k.boundary == 4;
+        for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
+                          [&](int j, const float* d, float r2, int sidx) {
+            const float4 hj = p.hi[j];
+            const int tj = tf_type(p.lo[j].w);
+            const float4 vtj = t.vt[j];
+            const float r = sqrtf(r2);
+            const float gf = w_grad(k, r);
+            const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = vti.z - vtj.z;
+            // continuity: m_Vj (v_i - v_j) . (L_i grad W)
+            const float gx = gf * d[0], gy = gf * d[1], gz = DIM == 3 ? gf * d[2] : 0.f;
+            if (CORR) {
+                const float cx = L[0] * gx + L[1] * gy + (DIM == 3 ? L[2] * gz : 0.f);
+                const float cy = L[3] * gx + L[4] * gy + (DIM == 3 ? L[5] * gz : 0.f);
+                const float cz = DIM == 3 ? L[6] * gx + L[7] * gy + L[8] * gz : 0.f;
+                dd.add(hj.w * (dvx * cx + dvy * cy + (DIM == 3 ? dvz * cz : 0.f)));
+            } else {
+                dd.add(hj.w * (dvx * gx + dvy * gy + (DIM == 3 ? dvz * gz : 0.f)));
+            }
+            // viscosity (fluid or boundary neighbours) and pressure, on the uncorrected gradient
+            const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
+            float cv = k.visc_fac * hj.w * fminf(vdx, 0.f) / (r2 + k.eps_h2);
+            if (tj != MAT_FLUID) cv = (tj == MAT_DUMMY || tj == MAT_REP || tj == MAT_RIGID) ? cv * visc_b : 0.f;
+            const float cp = -k.rho0 * hj.w * (vti.w + vtj.w);
+            float sc = (cv + cp) * gf;
+            float rs = 0.f;
+            if (rep_on && tj == MAT_REP) {  // repulsive force (eng/solver_sph_base.py:675-689)
+                const float chi = (r > 0.f && r < k.diam) ? 1.f - r / k.diam : 0.f;
+                const float gm = r / k.h075;
+                float f = 0.f;
+                if (gm > 0.f && gm <= 2.f / 3.f) f = 2.f / 3.f;
+                else if (gm > 2.f / 3.f && gm <= 1.f) f = 2.f * gm - 1.5f * gm * gm;
+                else if (gm > 1.f && gm < 2.f) f = 0.5f * (2.f - gm) * (2.f - gm);
+                rs = k.rep_fac * chi * f / r2;
+            }
+            sc += rs;
+            dv[0].add(sc * d[0]);
+            dv[1].add(sc * d[1]);
+            if (DIM == 3) dv[2].add(sc * d[2]);
+            if ((sidx & 7) == 7) { dd.flush(); dv[0].flush(); dv[1].flush(); dv[2].flush(); }
+        });
+        t.dd[i] = dd.get() * rti;
+        t.dv[i] = make_float4(dv[0].get() + k.g[0], dv[1].get() + k.g[1],
+                              (DIM == 3 ? dv[2].get() : 0.f) + k.g[2], 0.f);
+      }
     });
-    t.dd[i] = dd.get() * rti;
-    t.dv[i] = make_float4(dv[0].get() + rep[0] + k.g[0], dv[1].get() + rep[1] + k.g[1],
-                          (DIM == 3 ? dv[2].get() + rep[2] : 0.f) + k.g[2], 0.f);
 }
 
 // ---------------------------------------------------------------- integrators
@@ -635,26 +687,27 @@ __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
     if (!isfinite(dr)) atomicOr(err, TSG_ERR_NONFINITE);
 }
 
-template <int DIM>
+template <int DIM, bool FB>
 __global__ void k_xsph32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
-                         const int* __restrict__ sstart) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.nd) return;
-    const int ti = tf_type(p.lo[i].w);
-    if (!(ti > 0 && tf_dyn(p.lo[i].w))) return;
-    const float4 vi = p.vel[i];
-    CSum s[3];
-    for_list<DIM>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, is_flow(ti),
-                  [&](int j, const float*, float r2, int sidx) {
-        if (tf_type(p.lo[j].w) != ti) return;
-        const float w = w_val(k, sqrtf(r2)) * p.hi[j].w;
-        const float4 vj = p.vel[j];
-        s[0].add(w * (vj.x - vi.x));
-        s[1].add(w * (vj.y - vi.y));
-        if (DIM == 3) s[2].add(w * (vj.z - vi.z));
-        if ((sidx & 7) == 7) { s[0].flush(); s[1].flush(); s[2].flush(); }
+                         const int* __restrict__ sstart, Ovf ovf) {
+    FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
+        const int ti = tf_type(p.lo[i].w);
+        if (ti > 0 && tf_dyn(p.lo[i].w)) {
+            const float4 vi = p.vel[i];
+            CSum s[3];
+            for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, is_flow(ti),
+                              [&](int j, const float*, float r2, int sidx) {
+                if (tf_type(p.lo[j].w) != ti) return;
+                const float w = w_val(k, sqrtf(r2)) * p.hi[j].w;
+                const float4 vj = p.vel[j];
+                s[0].add(w * (vj.x - vi.x));
+                s[1].add(w * (vj.y - vi.y));
+                if (DIM == 3) s[2].add(w * (vj.z - vi.z));
+                if ((sidx & 7) == 7) { s[0].flush(); s[1].flush(); s[2].flush(); }
+            });
+            t.xs[i] = make_float4(s[0].get(), s[1].get(), DIM == 3 ? s[2].get() : 0.f, 0.f);
+        }
     });
-    t.xs[i] = make_float4(s[0].get(), s[1].get(), DIM == 3 ? s[2].get() : 0.f, 0.f);
 }
 
 __global__ void k_advect_pos32(K32 k, P32 p, T32 t, int* err) {
@@ -921,6 +974,8 @@ struct Fp32State {
     float4* pf = nullptr;
     int *dcount = nullptr, *dstart = nullptr, *scount = nullptr, *sstart = nullptr;
     int *cell_of = nullptr, *rank = nullptr, *perm = nullptr, *tiles = nullptr, *err = nullptr;
+    int *cells_d = nullptr, *cells_s = nullptr, *ncells = nullptr;  // non-empty cells (dynamic, static)
+    int *ovf_list = nullptr, *novf = nullptr;  // particles whose neighbours exceed the list capacity
     double* stage = nullptr;       // f64 export staging (9 n)
     double* scratch = nullptr;
     std::vector<void*> allocs;
@@ -1004,6 +1059,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     }
     k.G = c.G; k.grid = c.grid;
     k.Q = pow2_quantum(c.grid);
+    k.inv_grid = (float)(1.0 / c.grid);
     k.h1 = (float)c.h1;
     k.kk = (float)c.kk;
     k.kk6 = (float)(c.kk / 6.0);
@@ -1045,6 +1101,8 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     st->scount = dal<int>(*st, nb); st->sstart = dal<int>(*st, nb + 1);
     st->cell_of = dal<int>(*st, n); st->rank = dal<int>(*st, n); st->perm = dal<int>(*st, n);
     st->tiles = dal<int>(*st, nb / 2048 + 4); st->err = dal<int>(*st, 1);
+    st->cells_d = dal<int>(*st, nb); st->cells_s = dal<int>(*st, nb); st->ncells = dal<int>(*st, 2);
+    st->ovf_list = dal<int>(*st, n); st->novf = dal<int>(*st, 1);
     st->stage = dal<double>(*st, 9 * (size_t)n + 16);
     st->scratch = dal<double>(*st, 64);
     if (!t.nbr || !st->stage) { fp32_destroy(st); return TSG_E_CUDA; }
@@ -1096,6 +1154,8 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     } else {
         cudaMemsetAsync(st->sstart, 0, sizeof(int) * (c.G + 2), s);
     }
+    cudaMemsetAsync(st->ncells + 1, 0, sizeof(int), s);
+    TSG_LAUNCH(k_nonempty_cells, nblk(c.G, 256), 256, s, (long long)c.G, st->sstart, st->cells_s, st->ncells + 1);
     // the dynamic block of both buffers must agree before the first sort
     cudaStreamSynchronize(s);
     if (cudaGetLastError() != cudaSuccess) { fp32_destroy(st); return TSG_E_CUDA; }
@@ -1123,19 +1183,25 @@ void fp32_sort(Fp32State& st, cudaStream_t s) {
     P32& p = st.P[st.cur];
     {
         PhaseScope ph2(s, PH_LISTS);
+        cudaMemsetAsync(st.novf, 0, sizeof(int), s);
         if (k.dim == 3) {
-            const int nb = (int)((k.G + 3) / 4);
-            TSG_LAUNCH(k_lists_cell<3>, nb, 128, s, k, 0, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr);
-            TSG_LAUNCH(k_lists_cell<3>, nb, 128, s, k, 1, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr);
+            cudaMemsetAsync(st.ncells, 0, sizeof(int), s);
+            TSG_LAUNCH(k_nonempty_cells, nblk(k.G, 256), 256, s, (long long)k.G, st.dstart, st.cells_d, st.ncells);
+            const int nb = 152 * 16;
+            TSG_LAUNCH(k_lists_cell<3>, nb, 128, s, k, 0, st.cells_d, st.ncells, p.hi, p.lo, st.pf, st.dstart,
+                       st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
+            TSG_LAUNCH(k_lists_cell<3>, nb, 128, s, k, 1, st.cells_s, st.ncells + 1, p.hi, p.lo, st.pf, st.dstart,
+                       st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
             // particles in the out-of-grid bins (bounds read on the device)
             TSG_LAUNCH(k_lists_range<3>, 64, TPB, s, k, st.dstart + k.G, p.hi, p.lo, st.pf, st.dstart,
-                       st.sstart, st.T.cnt, st.T.nbr);
+                       st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
             TSG_LAUNCH(k_lists_range<3>, 64, TPB, s, k, st.sstart + k.G, p.hi, p.lo, st.pf, st.dstart,
-                       st.sstart, st.T.cnt, st.T.nbr);
+                       st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
             TSG_LAUNCH(k_lists_fixup<3>, 2 * 152, TPB, s, k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt,
-                       st.T.nbr);
+                       st.T.nbr, st.ovf_list, st.novf);
         } else {
-            DISPATCH32(k, k_lists, nblk(k.n), k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr);
+            TSG_LAUNCH(k_lists<2>, nblk(k.n), TPB, s, k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr,
+                       st.ovf_list, st.novf);
         }
     }
     st.lists_valid = true;
@@ -1144,7 +1210,14 @@ void fp32_sort(Fp32State& st, cudaStream_t s) {
 void fp32_kernel_corr(Fp32State& st, cudaStream_t s) {
     PhaseScope ph(s, PH_CORR);
     const K32& k = st.k;
-    DISPATCH32(k, k_corr32, nblk(k.n), k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart);
+    const Ovf ovf{st.ovf_list, st.novf};
+    if (k.dim == 2) {
+        TSG_LAUNCH((k_corr32<2, false>), nblk(k.n), TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
+        TSG_LAUNCH((k_corr32<2, true>), 64, TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
+    } else {
+        TSG_LAUNCH((k_corr32<3, false>), nblk(k.n), TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
+        TSG_LAUNCH((k_corr32<3, true>), 64, TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
+    }
 }
 
 void fp32_init_tmp(Fp32State& st, cudaStream_t s) {
@@ -1161,13 +1234,35 @@ void fp32_one_step(Fp32State& st, cudaStream_t s) {
     }
     {
         PhaseScope ph(s, PH_BDY);
-        if (k.n - k.nd > 0) DISPATCH32(k, k_bdy32, nblk(k.n - k.nd), k, p, st.T, st.pf, st.dstart, st.sstart, k.nd, k.n - k.nd);
-        if (st.c.n_bdy > k.n - k.nd)  // kinematic rigid particles live in the dynamic block
-            DISPATCH32(k, k_bdy32, nblk(k.nd), k, p, st.T, st.pf, st.dstart, st.sstart, 0, k.nd);
+        const Ovf ovf{st.ovf_list, st.novf};
+        auto bdy = [&](int base, int count_n) {
+            if (count_n <= 0) return;
+            if (k.dim == 2) {
+                TSG_LAUNCH((k_bdy32<2, false>), nblk(count_n), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+                TSG_LAUNCH((k_bdy32<2, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+            } else {
+                TSG_LAUNCH((k_bdy32<3, false>), nblk(count_n), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+                TSG_LAUNCH((k_bdy32<3, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+            }
+        };
+        bdy(k.nd, k.n - k.nd);
+        if (st.c.n_bdy > k.n - k.nd) bdy(0, k.nd);  // kinematic rigid particles live in the dynamic block
     }
     {
         PhaseScope ph(s, PH_RATES);
-        DISPATCH32(k, k_rates32, nblk(k.nd), k, p, st.T, st.pf, st.dstart, st.sstart);
+        const Ovf ovf{st.ovf_list, st.novf};
+        const int nb = nblk(k.nd);
+        if (k.dim == 2) {
+            if (k.corr) { TSG_LAUNCH((k_rates32<2, false, true>), nb, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                          TSG_LAUNCH((k_rates32<2, true, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
+            else { TSG_LAUNCH((k_rates32<2, false, false>), nb, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                   TSG_LAUNCH((k_rates32<2, true, false>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
+        } else {
+            if (k.corr) { TSG_LAUNCH((k_rates32<3, false, true>), nb, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                          TSG_LAUNCH((k_rates32<3, true, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
+            else { TSG_LAUNCH((k_rates32<3, false, false>), nb, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                   TSG_LAUNCH((k_rates32<3, true, false>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
+        }
     }
 }
 
@@ -1179,7 +1274,16 @@ void fp32_advect(Fp32State& st, int which, cudaStream_t s) {
     case TSG_ADVECT_LF_HALF: { PhaseScope ph(s, PH_INTEGRATE); TSG_LAUNCH(k_advect_half32, nblk(k.nd), TPB, s, k, p, st.T); break; }
     case TSG_ADVECT_POS: {
         PhaseScope ph(s, PH_POS);
-        if (k.xsph) DISPATCH32(k, k_xsph32, nblk(k.nd), k, p, st.T, st.pf, st.dstart, st.sstart);
+        if (k.xsph) {
+            const Ovf ovf{st.ovf_list, st.novf};
+            if (k.dim == 2) {
+                TSG_LAUNCH((k_xsph32<2, false>), nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                TSG_LAUNCH((k_xsph32<2, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+            } else {
+                TSG_LAUNCH((k_xsph32<3, false>), nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                TSG_LAUNCH((k_xsph32<3, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+            }
+        }
         TSG_LAUNCH(k_advect_pos32, nblk(k.nd), TPB, s, k, p, st.T, st.err);
         st.lists_valid = false;
         break;
