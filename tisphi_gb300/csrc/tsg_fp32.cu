@@ -79,6 +79,10 @@ __device__ __forceinline__ long long cell_coord(const K32& k, float hi, float lo
     return (long long)(int)t;
 }
 
+// |x| from |x|^2 through the hardware reciprocal square root (~2 ulp; 0 -> NaN, which the
+// kernel functions' support test rejects).
+__device__ __forceinline__ float fast_sqrt(float r2) { return r2 * rsqrtf(r2); }
+
 // Kernel value and gradient factor: W(r) and G with grad W = G * dx.
 __device__ __forceinline__ float w_val(const K32& k, float r) {
     float q = r * k.h1;
@@ -99,7 +103,7 @@ __device__ __forceinline__ float w_grad(const K32& k, float r) {
         float q1 = 1.f - 0.5f * q;
         return k.wgrad * (q1 * q1 * q1);                // -5 k h1^2 q1^3
     }
-    float inv = 1.f / r;
+    const float inv = __fdividef(1.f, r);
     if (q <= 1.f) return k.cub1 * q * (1.5f * q - 2.f) * inv;   // k h1 q (1.5 q - 2) / r
     float f = 2.f - q;
     return k.cub2 * f * f * inv;                       // -0.5 k h1 f^2 / r
@@ -321,8 +325,7 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
                              const float4* __restrict__ PF, const int* __restrict__ dstart,
                              const int* __restrict__ sstart, int* __restrict__ cnt, int* __restrict__ nbr,
                              int* __restrict__ ovf_list, int* __restrict__ novf) {
-    __shared__ float4 sh_hi[4][32];
-    __shared__ float4 sh_lo[4][32];
+    __shared__ float4 sh_rel[4][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int* own = self_blk == 0 ? dstart : sstart;
     const int ncell = *cell_count;
@@ -331,20 +334,26 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
     const long long c = cells[w];
     const int cb = own[c], ce = own[c + 1];
     const long long cx = c / (ny * nz), cy = (c / nz) % ny, cz = c % nz;
+    // reference quantum of this cell: positions are staged as (hi - ref) + lo, exact in hi - ref
+    const float4 ref = HI[cb];
     for (int p0 = cb; p0 < ce; p0 += 32) {
         const int i = p0 + lane;
         const bool active = i < ce;
-        float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
+        float rx = 0.f, ry = 0.f, rz = 0.f;
         bool flow_i = false, alias = false;
         if (active) {
-            hi_i = HI[i];
-            lo_i = LO[i];
+            const float4 hi_i = HI[i], lo_i = LO[i];
             flow_i = is_flow(tf_type(lo_i.w));
             bool ok = true;
             alias = cell_coord(k, hi_i.x, lo_i.x, ok) != cx || cell_coord(k, hi_i.y, lo_i.y, ok) != cy ||
                     cell_coord(k, hi_i.z, lo_i.z, ok) != cz || !ok;
+            rx = (hi_i.x - ref.x) + lo_i.x;
+            ry = (hi_i.y - ref.y) + lo_i.y;
+            rz = (hi_i.z - ref.z) + lo_i.z;
         }
         int m = 0;
+        int* wp = nbr + (active ? i : 0);
+        const size_t stride = (size_t)k.n;
         const bool any_flow = __any_sync(0xffffffffu, active && flow_i && !alias);
         for (int blk = 0; blk < (any_flow ? 2 : 1); ++blk) {
             const int* cs = blk == 0 ? dstart : sstart;
@@ -360,27 +369,26 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
                     for (int base = rb; base < re; base += 32) {
                         const int jj = base + lane;
                         if (jj < re) {
-                            sh_hi[wib][lane] = HI[jj];
-                            sh_lo[wib][lane] = LO[jj];
+                            const float4 hj = HI[jj], lj = LO[jj];
+                            sh_rel[wib][lane] = make_float4((hj.x - ref.x) + lj.x, (hj.y - ref.y) + lj.y,
+                                                            (hj.z - ref.z) + lj.z, lj.w);
                         }
                         __syncwarp();
                         const int mm = re - base < 32 ? re - base : 32;
                         if (active && !alias && (blk == 0 || flow_i)) {
-#pragma unroll 4
+#pragma unroll 8
                             for (int t = 0; t < mm; ++t) {
-                                const float4 hj = sh_hi[wib][t], lj = sh_lo[wib][t];
-                                const int j = base + t;
-                                if (j == i) continue;
-                                if (!flow_i && !is_flow(tf_type(lj.w))) continue;
-                                const float dx = (hi_i.x - hj.x) + (lo_i.x - lj.x);
-                                const float dy = (hi_i.y - hj.y) + (lo_i.y - lj.y);
+                                const float4 q = sh_rel[wib][t];
+                                const float dx = rx - q.x, dy = ry - q.y;
                                 float r2 = dx * dx + dy * dy;
                                 if (DIM == 3) {
-                                    const float dz = (hi_i.z - hj.z) + (lo_i.z - lj.z);
+                                    const float dz = rz - q.z;
                                     r2 += dz * dz;
                                 }
-                                if (r2 < k.R2) {
-                                    if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
+                                const int j = base + t;
+                                const bool ok_type = flow_i || is_flow(tf_type(q.w));
+                                if (r2 < k.R2 && j != i && ok_type) {
+                                    if (m < k.maxn) { *wp = j; wp += stride; }
                                     ++m;
                                 }
                             }
@@ -504,7 +512,7 @@ __global__ void k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, con
                           [&](int j, const float* d, float r2, int sidx) {
             const float4 hj = p.hi[j];
             const int tj = tf_type(p.lo[j].w);
-            const float r = sqrtf(r2);
+            const float r = fast_sqrt(r2);
             if (is_flow(tj)) s.add(hj.w * w_val(k, r));
             if ((sidx & 7) == 7) s.flush();
             if (want_L && tj == ti) {
@@ -573,7 +581,7 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
             const float4 hi_i = p.hi[i], lo_i = p.lo[i];
             for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
                               [&](int j, const float* d, float r2, int sidx) {
-                const float w = w_val(k, sqrtf(r2));
+                const float w = w_val(k, fast_sqrt(r2));
                 const float mV = p.hi[j].w;
                 const float4 vt = t.vt[j];
                 const float2 pr = t.pr[j];
@@ -617,7 +625,7 @@ __global__ void k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, co
             const float4 hj = p.hi[j];
             const int tj = tf_type(p.lo[j].w);
             const float4 vtj = t.vt[j];
-            const float r = sqrtf(r2);
+            const float r = fast_sqrt(r2);
             const float gf = w_grad(k, r);
             const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = vti.z - vtj.z;
             // continuity: m_Vj (v_i - v_j) . (L_i grad W)
@@ -632,8 +640,10 @@ __global__ void k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, co
             }
             // viscosity (fluid or boundary neighbours) and pressure, on the uncorrected gradient
             const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
-            float cv = k.visc_fac * hj.w * fminf(vdx, 0.f) / (r2 + k.eps_h2);
-            if (tj != MAT_FLUID) cv = (tj == MAT_DUMMY || tj == MAT_REP || tj == MAT_RIGID) ? cv * visc_b : 0.f;
+            // WCSPH scenes hold fluid, dummy, repulsive and rigid particles only (soil is rejected
+            // at upload), so every non-fluid neighbour takes the boundary form
+            const float cv = __fdividef(k.visc_fac * hj.w * fminf(vdx, 0.f), r2 + k.eps_h2) *
+                             (tj == MAT_FLUID ? 1.f : visc_b);
             const float cp = -k.rho0 * hj.w * (vti.w + vtj.w);
             float sc = (cv + cp) * gf;
             float rs = 0.f;
@@ -698,7 +708,7 @@ __global__ void k_xsph32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, con
             for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, is_flow(ti),
                               [&](int j, const float*, float r2, int sidx) {
                 if (tf_type(p.lo[j].w) != ti) return;
-                const float w = w_val(k, sqrtf(r2)) * p.hi[j].w;
+                const float w = w_val(k, fast_sqrt(r2)) * p.hi[j].w;
                 const float4 vj = p.vel[j];
                 s[0].add(w * (vj.x - vi.x));
                 s[1].add(w * (vj.y - vi.y));
