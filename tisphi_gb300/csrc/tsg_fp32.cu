@@ -178,11 +178,25 @@ __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restr
     if (!FB) {
         const int m = cnt[i];
         const float4 hi_i = HI[i], lo_i = LO[i];
-        int jn = m > 0 ? nbr[i] : 0;
-#pragma unroll 2
-        for (int s = 0; s < m; ++s) {
-            const int j = jn;
-            if (s + 1 < m) jn = nbr[(size_t)(s + 1) * k.n + i];
+        const size_t stride = (size_t)k.n;
+        const int* lp = nbr + i;
+        // two neighbours per trip: both index loads, then both position loads, then compute
+        int s = 0;
+        for (; s + 1 < m; s += 2) {
+            const int j0 = lp[0], j1 = lp[stride];
+            lp += 2 * stride;
+            const float4 h0 = HI[j0], l0 = LO[j0], h1 = HI[j1], l1 = LO[j1];
+            float d0[3], d1[3];
+            delta<DIM>(hi_i, lo_i, h0, l0, d0);
+            delta<DIM>(hi_i, lo_i, h1, l1, d1);
+            float r20 = d0[0] * d0[0] + d0[1] * d0[1];
+            float r21 = d1[0] * d1[0] + d1[1] * d1[1];
+            if (DIM == 3) { r20 += d0[2] * d0[2]; r21 += d1[2] * d1[2]; }
+            body(j0, d0, r20, s);
+            body(j1, d1, r21, s + 1);
+        }
+        if (s < m) {
+            const int j = lp[0];
             float d[3];
             delta<DIM>(hi_i, lo_i, HI[j], LO[j], d);
             float r2 = d[0] * d[0] + d[1] * d[1];
