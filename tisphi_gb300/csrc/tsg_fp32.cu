@@ -390,8 +390,11 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
                         __syncwarp();
                         const int mm = re - base < 32 ? re - base : 32;
                         if (active && !alias && (blk == 0 || flow_i)) {
+                            // test all staged candidates first (no stores in this loop, so the
+                            // shared loads pipeline), then write the accepted ones
+                            unsigned acc = 0u;
 #pragma unroll 8
-                            for (int t = 0; t < mm; ++t) {
+                            for (int t = 0; t < 32; ++t) {
                                 const float4 q = sh_rel[wib][t];
                                 const float dx = rx - q.x, dy = ry - q.y;
                                 float r2 = dx * dx + dy * dy;
@@ -399,12 +402,15 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
                                     const float dz = rz - q.z;
                                     r2 += dz * dz;
                                 }
-                                const int j = base + t;
                                 const bool ok_type = flow_i || is_flow(tf_type(q.w));
-                                if (r2 < k.R2 && j != i && ok_type) {
-                                    if (m < k.maxn) { *wp = j; wp += stride; }
-                                    ++m;
-                                }
+                                acc |= (t < mm && r2 < k.R2 && ok_type) ? (1u << t) : 0u;
+                            }
+                            if (i >= base && i < base + 32) acc &= ~(1u << (i - base));
+                            while (acc) {
+                                const int t = __ffs(acc) - 1;
+                                acc &= acc - 1u;
+                                if (m < k.maxn) { *wp = base + t; wp += stride; }
+                                ++m;
                             }
                         }
                         __syncwarp();
