@@ -92,6 +92,10 @@ typedef struct tsg_config {
     double poisson;
     double dilatancy;          /* rad */
     double damping_eps;        /* viscous damping coefficient (eng/solver_sph_base.py:714) */
+    double list_skin;          /* FP32-mixed: neighbour-list skin as a fraction of the support
+                                  radius; lists are rebuilt (and particles re-sorted) when a
+                                  particle has moved 0.45 skin since the last build; 0 = every
+                                  step.  Ignored by the FP64 form, which sorts every step. */
 } tsg_config;
 
 /* Initial particle set (eng/particle_system.py:289-314 _add_particles). */
@@ -167,7 +171,8 @@ int64_t tsg_particle_num(const tsg_handle* h);
 /* Cell offsets after the last sort: out[c] = inclusive end offset of cell c for
  * c < grid_num_total, out[grid_num_total] = n (the trailing out-of-grid bin).  Mirrors
  * grid_particle_num after the prefix sum (eng/particle_system.py:118, :256).  Host copy;
- * synchronises the stream. */
+ * synchronises the stream.  FP64 form only (the FP32-mixed form keeps its own cell tables
+ * for its real and boundary particle blocks): TSG_E_UNSUPPORTED otherwise. */
 int tsg_grid(tsg_handle* h, int32_t* out, void* stream);
 
 /* Neighbour lists in the reference's traversal order (for_all_neighbors,

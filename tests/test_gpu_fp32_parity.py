@@ -118,9 +118,13 @@ def test_one_step_rates_close(oracle_lib, native, scene, corr):
         assert err < 1e-4, f"{name}: normwise error {err:.3e}"
 
 
-@pytest.mark.parametrize("scene,ti", [("2d", 2), ("2d", 1), ("3d", 2)])
-def test_steps_density_position(oracle_lib, native, scene, ti):
+@pytest.mark.parametrize("scene,ti,skin", [("2d", 2, 0.1), ("2d", 1, 0.1), ("3d", 2, 0.1), ("2d", 2, 0.0),
+                                           ("3d", 2, 0.0), ("2d", 2, 0.002)])
+def test_steps_density_position(oracle_lib, native, scene, ti, skin):
+    """Neighbour-list skin 0.1 R: lists reused across steps; 0: rebuilt every step; 0.002 R:
+    rebuilt whenever a particle moves 0.0009 R (several rebuilds within the run)."""
     d = small_dambreak_2d(integration=ti) if scene == "2d" else small_dambreak_3d(integration=ti)
+    d["Configuration"]["neighbourSkin"] = skin
     sim, orc = _pair(d, oracle_lib)
     _advance(sim, orc, oracle_lib, 10)
     f = orc.get("mat_type") == 1

@@ -32,7 +32,7 @@ class tsg_config(ctypes.Structure):
         ("density0", ctypes.c_double), ("viscosity", ctypes.c_double), ("stiffness", ctypes.c_double),
         ("exponent", ctypes.c_double), ("cohesion", ctypes.c_double), ("friction", ctypes.c_double),
         ("E", ctypes.c_double), ("poisson", ctypes.c_double), ("dilatancy", ctypes.c_double),
-        ("damping_eps", ctypes.c_double),
+        ("damping_eps", ctypes.c_double), ("list_skin", ctypes.c_double),
     ]
 
 

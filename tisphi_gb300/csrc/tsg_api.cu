@@ -422,7 +422,9 @@ int tsg_step(tsg_handle* h, int nsteps, void* stream) {
     const bool collide = h->c.boundary == 1;
     for (int k = 0; k < nsteps; ++k) {
         int rc;
-        if ((rc = tsg_sort(h, stream))) return rc;
+        // FP32-mixed with a neighbour skin re-sorts only when its lists expire
+        if (!use_fp32(h) || fp32_rebuild_due(*h->f32, S(stream)))
+            if ((rc = tsg_sort(h, stream))) return rc;
         if ((rc = tsg_kernel_corr(h, stream))) return rc;
         if ((rc = tsg_init_tmp(h, stream))) return rc;
         if ((rc = tsg_substep(h, stream))) return rc;
@@ -568,8 +570,9 @@ int tsg_profile_read(double* ms, int64_t* counts, int nphase) {
 
 int tsg_grid(tsg_handle* h, int32_t* out, void* stream) {
     if (!h || !out || !h->sorted) return TSG_E_STATE;
+    if (use_fp32(h)) return TSG_E_UNSUPPORTED;  // the FP32-mixed form keeps its own cell tables
     cudaStream_t s = S(stream);
-    const int* cs = use_fp32(h) ? fp32_cell_start(*h->f32) : h->g.cell_start;
+    const int* cs = h->g.cell_start;
     cudaMemcpyAsync(out, cs + 1, sizeof(int32_t) * (h->c.G + 1), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     return check_cuda();

@@ -46,6 +46,7 @@ struct K32 {
     long long G;
     double vs[3], grid;
     float Q, inv_grid, h1, kk, kk6, wgrad, cub1, cub2, R2, R2lo, R2hi, pf_lim;
+    float R2L, R2Lhi, disp2_limit;  // list radius (support + skin) and rebuild threshold
     float visc_fac, eps_h2, rho0, B, gamma, dt, hdt, g[3], rep_fac, diam, h075, r_eps;
     float ds[3], de[3];
 };
@@ -124,7 +125,9 @@ template <int DIM, class F>
 __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4* __restrict__ HI,
                                                const float4* __restrict__ LO, const float4* __restrict__ PF,
                                                const int* __restrict__ dstart, const int* __restrict__ sstart,
-                                               bool flow_i, F&& body) {
+                                               bool flow_i, F&& body, bool list_radius = false) {
+    const float cut2 = list_radius ? k.R2L : k.R2;
+    const float cut2hi = list_radius ? k.R2Lhi : k.R2hi;
     const float4 hi_i = HI[i], lo_i = LO[i], pf_i = PF[i];
     bool ok = true;
     const long long cc0 = cell_coord(k, hi_i.x, lo_i.x, ok);
@@ -154,13 +157,13 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
                         float fx = pf_i.x - pj.x, fy = pf_i.y - pj.y, fz = pf_i.z - pj.z;
                         r2f = fx * fx + fy * fy;
                         if (DIM == 3) r2f += fz * fz;
-                        if (r2f > k.R2hi) continue;
+                        if (r2f > cut2hi) continue;
                     }
                     float d[3];
                     delta<DIM>(hi_i, lo_i, HI[j], LO[j], d);
                     float r2 = d[0] * d[0] + d[1] * d[1];
                     if (DIM == 3) r2 += d[2] * d[2];
-                    if (!(r2 < k.R2)) continue;
+                    if (!(r2 < cut2)) continue;
                     body(j, d, r2);
                 }
             }
@@ -192,8 +195,8 @@ __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restr
             float r20 = d0[0] * d0[0] + d0[1] * d0[1];
             float r21 = d1[0] * d1[0] + d1[1] * d1[1];
             if (DIM == 3) { r20 += d0[2] * d0[2]; r21 += d1[2] * d1[2]; }
-            body(j0, d0, r20, s);
-            body(j1, d1, r21, s + 1);
+            if (r20 < k.R2) body(j0, d0, r20, s);        // lists hold support + skin
+            if (r21 < k.R2) body(j1, d1, r21, s + 1);
         }
         if (s < m) {
             const int j = lp[0];
@@ -201,7 +204,7 @@ __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restr
             delta<DIM>(hi_i, lo_i, HI[j], LO[j], d);
             float r2 = d[0] * d[0] + d[1] * d[1];
             if (DIM == 3) r2 += d[2] * d[2];
-            body(j, d, r2, s);
+            if (r2 < k.R2) body(j, d, r2, s);
         }
     } else {
         int s = 0;
@@ -323,7 +326,7 @@ __global__ void k_lists(K32 k, const float4* __restrict__ HI, const float4* __re
     enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float*, float) {
         if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
         ++m;
-    });
+    }, true);
     cnt[i] = m;
     if (m > k.maxn) note_overflow(ovf_list, novf, i);
 }
@@ -403,7 +406,7 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
                                     r2 += dz * dz;
                                 }
                                 const bool ok_type = flow_i || is_flow(tf_type(q.w));
-                                acc |= (t < mm && r2 < k.R2 && ok_type) ? (1u << t) : 0u;
+                                acc |= (t < mm && r2 < k.R2L && ok_type) ? (1u << t) : 0u;
                             }
                             if (i >= base && i < base + 32) acc &= ~(1u << (i - base));
                             while (acc) {
@@ -454,7 +457,7 @@ __global__ void k_lists_fixup(K32 k, const float4* __restrict__ HI, const float4
         enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float*, float) {
             if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
             ++m;
-        });
+        }, true);
         cnt[i] = m;
         if (m > k.maxn) note_overflow(ovf_list, novf, i);
     }
@@ -474,7 +477,7 @@ __global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float
         enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float*, float) {
             if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
             ++m;
-        });
+        }, true);
         cnt[i] = m;
         if (m > k.maxn) note_overflow(ovf_list, novf, i);
     }
@@ -971,9 +974,20 @@ __global__ void k_nbr_fill32(K32 k, const float4* HI, const float4* LO, const fl
                         [&](int j, const float*, float) { list[m++] = j; });
 }
 
-__global__ void k_nbr_count_ell(K32 k, const int* cnt, int* counts) {
+template <int DIM>
+__global__ void k_nbr_count_ell(K32 k, const float4* HI, const float4* LO, const int* cnt, const int* nbr, int* counts) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < k.n) counts[i] = cnt[i];
+    if (i >= k.n) return;
+    const int m = cnt[i] < k.maxn ? cnt[i] : k.maxn;
+    int c = 0;
+    for (int q = 0; q < m; ++q) {
+        const int j = nbr[(size_t)q * k.n + i];
+        float d[3];
+        delta<DIM>(HI[i], LO[i], HI[j], LO[j], d);
+        const float r2 = d[0] * d[0] + d[1] * d[1] + (DIM == 3 ? d[2] * d[2] : 0.f);
+        if (r2 < k.R2) ++c;
+    }
+    counts[i] = c;
 }
 
 template <int DIM>
@@ -982,13 +996,35 @@ __global__ void k_nbr_fill_ell(K32 k, const float4* HI, const float4* LO, const 
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     const int m = cnt[i];
+    int w = off[i];
     if (m <= k.maxn) {
-        for (int q = 0; q < m; ++q) list[off[i] + q] = nbr[(size_t)q * k.n + i];
+        for (int q = 0; q < m; ++q) {
+            const int j = nbr[(size_t)q * k.n + i];
+            float d[3];
+            delta<DIM>(HI[i], LO[i], HI[j], LO[j], d);
+            const float r2 = d[0] * d[0] + d[1] * d[1] + (DIM == 3 ? d[2] * d[2] : 0.f);
+            if (r2 < k.R2) list[w++] = j;
+        }
     } else {
-        int w = off[i];
         enum_neighbors<DIM>(k, i, HI, LO, PF, ds, ss, is_flow(tf_type(PF[i].w)),
                             [&](int j, const float*, float) { list[w++] = j; });
     }
+}
+
+// Largest squared displacement of a real particle since the last list build (pf holds the
+// build-time positions); float bits of non-negative values order like unsigned integers.
+__global__ void k_disp32(K32 k, const float4* __restrict__ HI, const float4* __restrict__ LO,
+                         const float4* __restrict__ PF, unsigned* __restrict__ maxd) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.f;
+    if (i < k.nd) {
+        const float4 h = HI[i], l = LO[i], f = PF[i];
+        const float dx = (h.x + l.x) - f.x, dy = (h.y + l.y) - f.y, dz = (h.z + l.z) - f.z;
+        d2 = dx * dx + dy * dy + dz * dz;
+        if (!(d2 == d2)) d2 = 3.0e38f;  // non-finite: force a rebuild (the hash flags it)
+    }
+    for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
+    if ((threadIdx.x & 31) == 0 && d2 > 0.f) atomicMax(maxd, __float_as_uint(d2));
 }
 
 }  // namespace
@@ -1006,6 +1042,8 @@ struct Fp32State {
     int *cell_of = nullptr, *rank = nullptr, *perm = nullptr, *tiles = nullptr, *err = nullptr;
     int *cells_d = nullptr, *cells_s = nullptr, *ncells = nullptr;  // non-empty cells (dynamic, static)
     int *ovf_list = nullptr, *novf = nullptr;  // particles whose neighbours exceed the list capacity
+    unsigned* maxdisp = nullptr;               // squared displacement since the last list build
+    bool built = false;
     double* stage = nullptr;       // f64 export staging (9 n)
     double* scratch = nullptr;
     std::vector<void*> allocs;
@@ -1088,8 +1126,6 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
         k.ds[d] = (float)c.ds[d]; k.de[d] = (float)c.de[d];
     }
     k.G = c.G; k.grid = c.grid;
-    k.Q = pow2_quantum(c.grid);
-    k.inv_grid = (float)(1.0 / c.grid);
     k.h1 = (float)c.h1;
     k.kk = (float)c.kk;
     k.kk6 = (float)(c.kk / 6.0);
@@ -1103,7 +1139,28 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     k.visc_fac = (float)c.visc_fac; k.eps_h2 = (float)c.eps_h2; k.rho0 = (float)c.rho0; k.B = (float)c.B;
     k.gamma = (float)c.gamma; k.dt = (float)c.dt; k.hdt = (float)c.hdt;
     k.rep_fac = (float)c.rep_fac; k.diam = (float)c.diam; k.h075 = (float)c.h075; k.r_eps = (float)c.r_eps;
-    k.maxn = ell_capacity(c.dim, c.R, cfg.particle_diameter);
+    // Verlet skin: lists hold pairs within R + skin and stay valid while no particle has moved
+    // more than skin / 2 since they were built (0.45 skin for margin on f32 positions)
+    const double skin = cfg.list_skin > 0 ? cfg.list_skin * c.R : 0.0;
+    const double RL = c.R + skin;
+    k.R2L = skin > 0 ? (float)(RL * RL) : k.R2;
+    k.R2Lhi = skin > 0 ? std::nextafter((float)(RL * RL * (1.0 + 1.0 / 1024.0)), 1e30f) : k.R2hi;
+    k.disp2_limit = skin > 0 ? (float)((0.45 * skin) * (0.45 * skin)) : 0.f;
+    k.maxn = ell_capacity(c.dim, RL, cfg.particle_diameter);
+    // internal cell grid: cells at least R + skin wide so that the 3^dim stencil covers the
+    // list radius; it spans the reference's virtual domain (neighbour sets do not depend on it)
+    if (RL > c.grid) {
+        k.grid = RL;
+        long long G = 1;
+        for (int d = 0; d < 3; ++d) {
+            if (d < c.dim) k.gnum[d] = (int)std::ceil((double)c.gnum[d] * c.grid / RL);
+            else k.gnum[d] = c.gnum[d];
+            if (d < c.dim) G *= k.gnum[d];
+        }
+        k.G = G;
+    }
+    k.Q = pow2_quantum(k.grid);
+    k.inv_grid = (float)(1.0 / k.grid);
     // host copies of the classification to place particles: dynamic block first
     std::vector<int32_t> mt(n);
     cudaMemcpy(mt.data(), pp->mat_type, sizeof(int32_t) * n, from_device ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost);
@@ -1126,13 +1183,14 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     t.cnt = dal<int>(*st, n);
     t.nbr = dal<int>(*st, (size_t)k.maxn * n);
     st->pf = dal<float4>(*st, n);
-    const size_t nb = (size_t)c.G + 1;
+    const size_t nb = (size_t)k.G + 1;
     st->dcount = dal<int>(*st, nb); st->dstart = dal<int>(*st, nb + 1);
     st->scount = dal<int>(*st, nb); st->sstart = dal<int>(*st, nb + 1);
     st->cell_of = dal<int>(*st, n); st->rank = dal<int>(*st, n); st->perm = dal<int>(*st, n);
     st->tiles = dal<int>(*st, nb / 2048 + 4); st->err = dal<int>(*st, 1);
     st->cells_d = dal<int>(*st, nb); st->cells_s = dal<int>(*st, nb); st->ncells = dal<int>(*st, 2);
     st->ovf_list = dal<int>(*st, n); st->novf = dal<int>(*st, 1);
+    st->maxdisp = dal<unsigned>(*st, 1);
     st->stage = dal<double>(*st, 9 * (size_t)n + 16);
     st->scratch = dal<double>(*st, 64);
     if (!t.nbr || !st->stage) { fp32_destroy(st); return TSG_E_CUDA; }
@@ -1169,7 +1227,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     // static block: sort once into P[1], copy the whole static block into both buffers
     if (n - nd > 0) {
         build_cells(*st, nd, n - nd, st->scount, st->sstart, s, true);
-        const long long m = c.G + 2;
+        const long long m = k.G + 2;
         TSG_LAUNCH(k_offset, nblk(m, 256), 256, s, st->sstart, m, nd);
         P32& src = st->P[1];
         P32& dst = st->P[0];
@@ -1182,10 +1240,10 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
         cudaMemcpyAsync(dst.mass + off, src.mass + off, sizeof(float) * ns, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(dst.ids + off, src.ids + off, sizeof(int4) * ns, cudaMemcpyDeviceToDevice, s);
     } else {
-        cudaMemsetAsync(st->sstart, 0, sizeof(int) * (c.G + 2), s);
+        cudaMemsetAsync(st->sstart, 0, sizeof(int) * (k.G + 2), s);
     }
     cudaMemsetAsync(st->ncells + 1, 0, sizeof(int), s);
-    TSG_LAUNCH(k_nonempty_cells, nblk(c.G, 256), 256, s, (long long)c.G, st->sstart, st->cells_s, st->ncells + 1);
+    TSG_LAUNCH(k_nonempty_cells, nblk(k.G, 256), 256, s, (long long)k.G, st->sstart, st->cells_s, st->ncells + 1);
     // the dynamic block of both buffers must agree before the first sort
     cudaStreamSynchronize(s);
     if (cudaGetLastError() != cudaSuccess) { fp32_destroy(st); return TSG_E_CUDA; }
@@ -1234,7 +1292,22 @@ void fp32_sort(Fp32State& st, cudaStream_t s) {
                        st.ovf_list, st.novf);
         }
     }
+    cudaMemsetAsync(st.maxdisp, 0, sizeof(unsigned), s);
     st.lists_valid = true;
+    st.built = true;
+}
+
+bool fp32_rebuild_due(Fp32State& st, cudaStream_t s) {
+    if (!st.built || st.k.disp2_limit <= 0.f) return true;
+    const K32& k = st.k;
+    P32& p = st.P[st.cur];
+    TSG_LAUNCH(k_disp32, nblk(k.nd), TPB, s, k, p.hi, p.lo, st.pf, st.maxdisp);
+    unsigned bits = 0;
+    cudaMemcpyAsync(&bits, st.maxdisp, sizeof bits, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    float d2;
+    std::memcpy(&d2, &bits, sizeof d2);
+    return !(d2 <= k.disp2_limit);
 }
 
 void fp32_kernel_corr(Fp32State& st, cudaStream_t s) {
@@ -1315,7 +1388,7 @@ void fp32_advect(Fp32State& st, int which, cudaStream_t s) {
             }
         }
         TSG_LAUNCH(k_advect_pos32, nblk(k.nd), TPB, s, k, p, st.T, st.err);
-        st.lists_valid = false;
+        if (k.disp2_limit <= 0.f) st.lists_valid = false;
         break;
     }
     case TSG_ADVECT_SOMETHING: { PhaseScope ph(s, PH_POST); TSG_LAUNCH(k_post_wc32, nblk(k.nd), TPB, s, k, p); break; }
@@ -1362,7 +1435,7 @@ void fp32_neighbors(Fp32State& st, int* counts, int* offsets, int* list, cudaStr
     const K32& k = st.k;
     P32& p = st.P[st.cur];
     if (st.lists_valid) {  // report the lists the physics kernels use
-        if (!list) TSG_LAUNCH(k_nbr_count_ell, nblk(k.n), TPB, s, k, st.T.cnt, counts);
+        if (!list) DISPATCH32(k, k_nbr_count_ell, nblk(k.n), k, p.hi, p.lo, st.T.cnt, st.T.nbr, counts);
         else DISPATCH32(k, k_nbr_fill_ell, nblk(k.n), k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt,
                         st.T.nbr, offsets, list);
         return;

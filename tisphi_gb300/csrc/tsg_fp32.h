@@ -10,6 +10,8 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* p, 
                 Fp32State** out, cudaStream_t s);
 void fp32_destroy(Fp32State* st);
 void fp32_sort(Fp32State& st, cudaStream_t s);
+// True when the neighbour lists must be rebuilt before the next step (always without a skin).
+bool fp32_rebuild_due(Fp32State& st, cudaStream_t s);
 void fp32_kernel_corr(Fp32State& st, cudaStream_t s);
 void fp32_init_tmp(Fp32State& st, cudaStream_t s);
 void fp32_one_step(Fp32State& st, cudaStream_t s);
