@@ -174,19 +174,38 @@ def cpu_baseline(cfg_dict, budget_s=25.0):
 
 
 # ---------------------------------------------------------------- GPU measurement
-def algorithmic_bytes_rates(n_total, n_flow, precision, corr):
-    """Unique bytes the rates kernel must move once per launch (neighbour re-reads excluded).
+def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None):
+    """Unique bytes a kernel must move once per launch (neighbour re-reads excluded).
 
-    FP64: every particle's x (24) + m_V (8) + v_tmp (24) + density_tmp (8) + pressure (8) +
-    mat_type (4) + f32 prefilter position (16) are read; each flow particle additionally
-    reads its list index (4) and CSPM matrix (72 when corrected) and writes d_density (8) and
-    d_vel (24).  FP32-mixed: position (16) + packed cell (4) + velocity/volume (16) +
-    density/pressure (8) per particle; per flow particle list (4) + CSPM (36 when corrected)
-    + writes (16).
+    Every per-particle array the kernel touches counts once (read or written), as does
+    every neighbour-list entry it reads (4 B each: the list is data the kernel streams, not
+    a re-read).  FP64 (cell traversal, no lists): rates read x (24) + m_V (8) + v_tmp (24) +
+    density_tmp (8) + pressure (8) + mat_type (4) + f32 prefilter position (16) of every
+    particle, and per flow particle its CSPM matrix (72 when corrected) plus the writes of
+    d_density (8) and d_vel (24).  FP32-mixed:
+      rates:  hi + lo + (v_tmp, p / rho^2) of every particle (48); per flow particle
+              density_tmp (4) + list count (4) + CSPM matrix (36 when corrected) + writes
+              d_density (4) and d_vel (16); plus the real particles' list entries;
+      corr:   hi + lo + count of every particle (36) + writes CSPM_f (4) and CSPM_L (36 when
+              corrected); plus every list entry;
+      boundary: per dummy hi + lo + velocity (48) + count (4) + writes (v_tmp, p) (16),
+              (p, rho) (8), density_tmp (4), pressure (4); per flow particle m_V + v_tmp +
+              (p, rho) (4 + 16 + 8); plus the dummies' list entries.
     """
+    n_dummy = n_total - n_flow
     if precision == "fp64":
+        if kernel != "rates":
+            return None
         return n_total * 92 + n_flow * (4 + (72 if corr else 0) + 32)
-    return n_total * 44 + n_flow * (4 + (36 if corr else 0) + 16)
+    lists = lists or {"entries_real": 0, "entries_dummy": 0}
+    er, ed = lists["entries_real"], lists["entries_dummy"]
+    if kernel == "rates":
+        return n_total * 48 + n_flow * (4 + 4 + (36 if corr else 0) + 20) + 4 * er
+    if kernel == "kernel_corr":
+        return n_total * (36 + 4 + (36 if corr else 0)) + 4 * (er + ed)
+    if kernel == "boundary":
+        return n_dummy * (48 + 4 + 32) + n_flow * 28 + 4 * ed
+    return None
 
 
 def measure(args, cfg_dict, precision, rank, dist):
@@ -208,6 +227,10 @@ def measure(args, cfg_dict, precision, rank, dist):
         solver.step()
     torch.cuda.synchronize()
     ps.check_errors()
+    try:
+        builds0 = ps.list_stats()["builds"]
+    except nat.NativeError:  # the FP64 form traverses cells and keeps no lists
+        builds0 = None
     # ---- timed region: K steps, CUDA events on the launch stream
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
@@ -226,6 +249,7 @@ def measure(args, cfg_dict, precision, rank, dist):
     ms = max_over_ranks(dist, ms)
     clocks = clk.summary()
     ps.check_errors()
+    timed_builds = ps.list_stats()["builds"] - builds0 if builds0 is not None else None
     # ---- per-phase kernel timing (separate pass of the same steps, events on the stream)
     lib.tsg_profile(1)
     for _ in range(args.steps):
@@ -265,17 +289,59 @@ def measure(args, cfg_dict, precision, rank, dist):
         e2e = {"value": n_fluid * e2e_steps / el, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": e2e_steps}
     diag = ps.diagnostics()
+    try:
+        list_stats = ps.list_stats()
+    except nat.NativeError:  # the FP64 form traverses cells and keeps no lists
+        list_stats = None
     del sim
     torch.cuda.synchronize()
-    lists = phases.get("neighbour_lists")
-    rebuilds = lists["launches"] if lists else 0
+    rebuilds = None
+    if timed_builds is not None:
+        rebuilds = {"in_timed_steps": timed_builds, "timed_steps": args.steps,
+                    "since_upload": list_stats["builds"] if list_stats else None,
+                    "steps_since_upload": 2 * args.steps + args.warmup + (e2e["steps"] if e2e else 0),
+                    "note": "FP32-mixed neighbour lists hold pairs within support + skin and are rebuilt "
+                            "(with the sort) only once a particle has moved 0.45 skin; the FP64 form "
+                            "sorts and traverses cells every step"}
     return {"ms_per_step": ms, "value": n_fluid / (ms * 1e-3), "launches": launches,
-            "list_rebuilds": {"per_step": rebuilds / args.steps,
-                              "note": "FP32-mixed neighbour lists carry a skin and are rebuilt (with the "
-                                      "sort) only when a particle has moved 0.45 skin; counted over "
-                                      "the profiled pass that follows the timed steps"},
+            "list_rebuilds": rebuilds,
             "launches_per_step": launches / args.steps, "clocks": clocks, "phases": phases, "e2e": e2e,
-            "n_total": n_total, "n_fluid": n_fluid, "diag_mass": diag["mass"]}
+            "n_total": n_total, "n_fluid": n_fluid, "diag_mass": diag["mass"], "lists": list_stats}
+
+
+def error_report(cfg_dict, checkpoints=(1, 20)):
+    """Per-field error of the FP32-mixed form against the FP64 form after 1 and 20 steps.
+
+    Both forms start from the same uploaded state.  The FP64 GPU form rounds every
+    operation like the f64 CPU oracle (the parity tests require bit-identical results), so
+    it stands in for the oracle at full size, where the oracle would need minutes.
+    """
+    import torch
+
+    from tisphi_gb300 import compare
+    from tisphi_gb300.configer_builder import SimConfiger
+    from tisphi_gb300.simulation import Simulation
+
+    sims = {p: Simulation(SimConfiger(config=cfg_dict), precision=p) for p in ("fp32_mixed", "fp64")}
+    d0 = {p: s.ps.diagnostics() for p, s in sims.items()}
+    out, done = {}, 0
+    for n in checkpoints:
+        for s in sims.values():
+            s.solver.step(n - done)
+        done = n
+        torch.cuda.synchronize()
+        rec = compare.field_errors(sims["fp32_mixed"].ps, sims["fp64"].ps)
+        dr = {p: compare.drift(d0[p], s.ps.diagnostics()) for p, s in sims.items()}
+        rec["conservation"] = {p: {"mass_rel": v["mass_rel"], "energy_rel": v["energy_rel"],
+                                   "front": v["front"]} for p, v in dr.items()}
+        out[f"after_{n}_steps"] = rec
+    del sims
+    torch.cuda.synchronize()
+    return {"reference": "FP64 GPU form (bit-identical to the f64 oracle in the parity tests)",
+            "matched_by": "id0", "particles": "fluid",
+            "definitions": "density: |a-b|/|b| per particle; pressure, v, d_density, d_vel: |a-b| / max|b| "
+                           "(Euclidean norm per particle for vectors); x: max |a-b| in metres",
+            **out}
 
 
 def read_profile_traffic(kernel_tag):
@@ -312,10 +378,17 @@ def run_ours(args):
     peak, peak_kind = hbm_peak()
     corr = cfg_dict["Configuration"]["kernelCorrection"] == 1
     n_flow = h["n_fluid"]
-    rates = h["phases"].get("rates", {"ms_per_launch": 0.0})
-    alg = algorithmic_bytes_rates(h["n_total"], n_flow, head, corr)
-    achieved = alg / (rates["ms_per_launch"] * 1e-3) / 1e9 if rates["ms_per_launch"] else 0.0
-    traffic = read_profile_traffic(f"rates_{head}_3d")
+    def roof(kernel):
+        ph = h["phases"].get(kernel)
+        alg = algorithmic_bytes(kernel, h["n_total"], n_flow, head, corr, h.get("lists"))
+        if not ph or not alg or not ph["ms_per_launch"]:
+            return None
+        ach = alg / (ph["ms_per_launch"] * 1e-3) / 1e9
+        return {"achieved": ach, "frac": ach / peak, "algorithmic_bytes_per_launch": alg,
+                "ms_per_launch": ph["ms_per_launch"]}
+    rates = roof("rates") or {"achieved": 0.0, "frac": 0.0, "algorithmic_bytes_per_launch": None,
+                              "ms_per_launch": 0.0}
+    traffic = read_profile_traffic(f"rates_{head}_3d_dambreak")
     line = {
         "metric": METRIC, "value": h["value"] * ws, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -327,24 +400,87 @@ def run_ours(args):
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "forms": {k: ({"value": v["value"], "ms_per_step": v["ms_per_step"]} if "value" in v else v)
                   for k, v in forms.items()},
-        "roofline": {"kernel": "rates (k_wc_rates)", "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": rates["ms_per_launch"],
-                     "traffic": traffic},
+        "roofline": {"kernel": "rates: continuity + momentum (k_rates32 / k_wc_rates)", "bound": "hbm",
+                     "achieved": rates["achieved"], "peak": peak, "unit": "GB/s", "frac": rates["frac"],
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": rates["algorithmic_bytes_per_launch"],
+                     "ms_per_launch": rates["ms_per_launch"], "traffic": traffic,
+                     "other_kernels": {k: roof(k) for k in ("kernel_corr", "boundary") if roof(k)}},
         "phases": h["phases"],
         "clocks": h["clocks"],
         "e2e": h["e2e"],
         "gpu_launches": int(h["launches"]),
         "list_rebuilds": h.get("list_rebuilds"),
+        "lists": h.get("lists"),
     }
     if "fp32_mixed" in forms and "fp64" in forms and "value" in forms["fp32_mixed"] and "value" in forms["fp64"]:
         line["speedup_fp32_mixed_vs_fp64"] = forms["fp32_mixed"]["value"] / forms["fp64"]["value"]
+    if rank == 0 and not args.no_errors and all("value" in forms.get(p, {}) for p in ("fp32_mixed", "fp64")):
+        line["errors"] = error_report(cfg_dict)
+        rel = line["errors"]["after_1_steps"].get("density", {}).get("max_rel")
+        line["config"]["density_rel_err_1_step"] = rel
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cfg_dict)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_batch(args):
+    """256-scene dambreak ensemble: one batched handle (graph replays, autotuned launch shape)
+    against the same scenes stepped one after another through their own handles."""
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    from tisphi_gb300 import build_native, scenes
+    build_native.build()
+    from tisphi_gb300.batch import SceneBatch
+    from tisphi_gb300.configer_builder import SimConfiger
+    from tisphi_gb300.simulation import Simulation
+    cfgs = scenes.dambreak_ensemble(args.scenes)
+    batch = SceneBatch(cfgs)
+    nf = int(batch.n_fluid.sum())
+    tuned = batch.autotune(trial_steps=10)
+    stream = torch.cuda.current_stream()
+    batch.step(args.warmup)
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        start.record(stream)
+        batch.step(args.steps)
+        stop.record(stream)
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(stop) / args.steps
+    batch.check_errors()
+    stats = batch.list_stats()
+    del batch
+    # sequential: every scene through its own handle, one after another
+    sims = [Simulation(SimConfiger(config=c), precision="fp32_mixed") for c in cfgs]
+    for s in sims:
+        s.solver.step(1)
+    torch.cuda.synchronize()
+    k_seq = max(1, min(args.steps, 10))
+    start.record(stream)
+    for s in sims:
+        s.solver.step(k_seq)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = start.elapsed_time(stop) / k_seq
+    line = {"metric": "scenes*steps/s, 256-scene 2D WCSPH dambreak ensemble, batched vs sequential",
+            "value": args.scenes / (ms * 1e-3), "unit": "scenes*steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"{args.scenes} 2D WCSPH dambreaks, spacing 0.01 m, block width U[0.3, 1.5] m, "
+                                   f"height U[0.2, 0.8] m, B log-U[2e4, 1e5], nu log-U[1e-3, 1e-2], seed 7, "
+                                   f"LF dt 1e-4", "n_fluid": nf,
+                       "l2": "working set ~0.15 GB > 129 MB L2 (no flush)"},
+            "launch": tuned, "particle_updates_per_s": nf / (ms * 1e-3),
+            "sequential": {"ms_per_step_all_scenes": ms_seq, "value": args.scenes / (ms_seq * 1e-3),
+                           "steps_timed": k_seq, "how": "each scene's own FP32-mixed handle, stepped in turn"},
+            "speedup_vs_sequential": ms_seq / ms, "lists": stats, "clocks": clk.summary()}
+    print(json.dumps(line))
 
 
 def run_reference(args):
@@ -396,15 +532,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["both", "fp32_mixed", "fp64"], default="both")
-    ap.add_argument("--workload", choices=["3d", "2d"], default="3d")
+    ap.add_argument("--workload", choices=["3d", "2d", "batch"], default="3d")
+    ap.add_argument("--scenes", type=int, default=256, help="ensemble size for --workload batch")
     ap.add_argument("--spacing", type=float, default=0.0054)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-errors", action="store_true", help="skip the FP32-mixed vs FP64 error report")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -187,6 +187,15 @@ int tsg_neighbors(tsg_handle* h, int32_t* counts, int32_t* list, int64_t cap, in
  * reference prints no conservation figures); synchronises. */
 int tsg_reduce_diag(tsg_handle* h, double out[8], void* stream);
 
+/* Neighbour-list occupancy of the FP32-mixed form (TSG_E_UNSUPPORTED for FP64, which
+ * traverses cells and keeps no lists): out[0] list entries stored for real particles
+ * (pairs within the support plus the skin), out[1] the same for dummy / repulsive
+ * particles, out[2] particles whose neighbours exceeded the list capacity (served by
+ * direct traversal), out[3] list builds since upload.
+ * No reference counterpart (the reference re-walks the cells in every loop); used for
+ * byte accounting and to report the rebuild rate.  Synchronises. */
+int tsg_list_stats(tsg_handle* h, int64_t out[4], void* stream);
+
 /* Device error word accumulated since the last call (and cleared).  Synchronises. */
 int tsg_last_error(tsg_handle* h, void* stream);
 
@@ -230,6 +239,47 @@ int tsg_profile_read(double* ms, int64_t* counts, int nphase);
 #define TSG_NOALLOC_MAX_CELLS 262144
 int tsg_sort_noalloc(const tsg_config* cfg, const double* x, int64_t n, int32_t* cell_start, int32_t* perm,
                      void* stream);
+
+/* Launch configuration of the FP32-mixed form.  No reference counterpart (Taichi picks
+ * its own launch shapes): threads_per_block of the neighbour-traversal kernels (64, 128,
+ * 256, 512); cells_per_cta of the neighbour-list build, one warp per cell (2, 4, 8; 0 = one
+ * thread per particle); steps_per_graph, how many steps one captured CUDA graph replays
+ * (1..64).  tsg_step runs FP32-mixed steps as graph replays (each step re-sorts inside the
+ * graph only when the device-side displacement check asks for it); while tsg_profile is
+ * on it runs them eagerly. */
+typedef struct tsg_launch_cfg {
+    int32_t threads_per_block;
+    int32_t cells_per_cta;
+    int32_t steps_per_graph;
+} tsg_launch_cfg;
+int tsg_set_launch(tsg_handle* h, const tsg_launch_cfg* cfg);
+int tsg_get_launch(tsg_handle* h, tsg_launch_cfg* cfg);
+
+/* Autotuner (no reference counterpart): times candidate launch configurations from the
+ * current state - threads per block over trial_steps full steps, cells per CTA over the
+ * re-sort + list build, steps per graph over full steps - keeps the fastest, writes it to
+ * *best and the best milliseconds per step to *ms_per_step (either may be NULL), and puts
+ * the particle state back as it was (re-sorted), so tuning does not advance the
+ * simulation.  Synchronises.  TSG_E_STATE while tsg_profile is on. */
+int tsg_autotune(tsg_handle* h, int32_t trial_steps, tsg_launch_cfg* best, double* ms_per_step, void* stream);
+
+/* Batched ensemble: nscenes independent WCSPH scenes stepped together by the same
+ * launches (no reference counterpart; the reference runs one scene per process).  Every
+ * scene must share dim, kernel, correction, integrator, dummy boundary (2), the FP32-mixed
+ * precision, the grid, spacing, dt, density0, exponent and gravity; stiffness and
+ * viscosity may differ per scene, particle counts may differ freely.  The scenes are
+ * placed side by side along x, scene q shifted by q * tsg_batch_pitch(h) (so fields read
+ * through tsg_field / tsg_read carry that shift), with a gap wider than the support
+ * radius plus the list skin, so no pair crosses scenes.  Particles are numbered scene by
+ * scene in the order given (id0).  parts are host arrays.  The handle then takes every
+ * ordinary entry point (tsg_step, tsg_field, tsg_autotune, ...).  At most 4096 scenes. */
+int tsg_batch_create(const tsg_config* cfgs, const tsg_particles* parts, int32_t nscenes, void* stream,
+                     tsg_handle** out);
+/* Per-scene FP64 diagnostics: out[8 * q + k] with k as in tsg_reduce_diag, positions
+ * relative to scene q's own origin.  Synchronises. */
+int tsg_batch_diag(tsg_handle* h, double* out, int32_t nscenes, void* stream);
+/* x shift between consecutive scenes of a batch (0 for an ordinary handle). */
+double tsg_batch_pitch(const tsg_handle* h);
 
 /* Human-readable text for a status code. */
 const char* tsg_status_string(int status);

@@ -1,0 +1,196 @@
+"""Batched ensembles, captured step graphs and the autotuner (FP32-mixed form).
+
+* A batch of dambreaks with different block sizes, stiffness and viscosity against the
+  same scenes run one by one: neighbour sets identical (integer, exact); after 10
+  leap-frog steps density within 1e-5 relative and positions within 1e-6 m (the FP32
+  tolerances; the batch walks a different cell grid, so f32 sums run in another order);
+  per-scene mass identical.
+* One batch scene against the f64 oracle with the same tolerances.
+* Graph replay against the eager step path (per-phase profiling forces eager steps):
+  bit-identical, since both launch the same kernels in the same order.
+* Threads per block changes no arithmetic: bit-identical.  Cells per CTA of the list
+  build (and the per-particle builder) give the same neighbour sets; the entries of a list
+  may be ordered differently, so steps agree within 1e-6 relative.
+* The autotuner restores the particle state: every field equal after tuning.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from helpers import cfg_of, small_dambreak_2d
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes():
+    from tisphi_gb300 import scenes
+    out = []
+    for q, (w, h, b, nu) in enumerate([(0.3, 0.2, 2e4, 1e-3), (0.6, 0.4, 5e4, 5e-3), (0.44, 0.3, 1e5, 1e-2)]):
+        out.append(scenes.dambreak_2d(spacing=0.02, width=w, height=h, stiffness=b, viscosity=nu, seed=11 + q,
+                                      domain=(1.2, 0.8)))
+    return out
+
+
+def _single(d):
+    from tisphi_gb300.simulation import Simulation
+    return Simulation(cfg_of(d), precision="fp32_mixed")
+
+
+def _by_id0(ps, name):
+    ids = ps.field("id0").cpu().numpy()
+    a = ps.field(name).cpu().numpy().astype(np.float64)
+    out = np.empty_like(a)
+    out[ids] = a
+    return out
+
+
+def test_batch_matches_single_scenes(native):
+    from tisphi_gb300.batch import SceneBatch
+    ds = _scenes()
+    batch = SceneBatch(ds)
+    singles = [_single(d) for d in ds]
+    batch.step(10)
+    for s in singles:
+        s.solver.step(10)
+    batch.check_errors()
+    diag = batch.diagnostics()
+    for q, s in enumerate(singles):
+        mt = _by_id0(s.ps, "mat_type")
+        f = mt == 1
+        rho_b = batch.scene_field("density", q)[f]
+        rho_s = _by_id0(s.ps, "density")[f]
+        assert np.max(np.abs(rho_b - rho_s) / rho_s) < 1e-5, f"scene {q} density"
+        x_b = batch.scene_field("x", q)[f]
+        x_s = _by_id0(s.ps, "x")[f]
+        assert np.max(np.abs(x_b - x_s)) < 1e-6, f"scene {q} positions"
+        d_s = s.ps.diagnostics()
+        assert diag[q]["mass"] == pytest.approx(d_s["mass"], rel=1e-12)
+        assert diag[q]["front"] == pytest.approx(d_s["front"], abs=1e-6)
+
+
+def test_batch_neighbor_sets_equal_single(native):
+    """Neighbour sets of the batch (through tsg_neighbors after the first sort) per scene
+    equal the scene's own, except pairs within 1e-6 R of the support radius, where the
+    f32 rounding of the shifted positions may decide differently."""
+    from tisphi_gb300 import _native as nat
+    from tisphi_gb300.batch import SceneBatch
+    ds = _scenes()
+    batch = SceneBatch(ds)
+    lib = nat.load()
+    nat.check(lib.tsg_sort(batch._h, None), "sort")
+    n = batch.n
+    counts = np.zeros(n, dtype=np.int32)
+    total = ctypes.c_int64()
+    nat.check(lib.tsg_neighbors(batch._h, nat.as_ptr(counts, ctypes.c_int32), None, 0, ctypes.byref(total), None),
+              "count")
+    lst = np.zeros(total.value, dtype=np.int32)
+    nat.check(lib.tsg_neighbors(batch._h, nat.as_ptr(counts, ctypes.c_int32), nat.as_ptr(lst, ctypes.c_int32),
+                                total.value, ctypes.byref(total), None), "fill")
+    gid = batch.field("id0").cpu().numpy()
+    off = np.concatenate([[0], np.cumsum(counts)])
+    pos_b = {int(g): k for k, g in enumerate(gid)}
+    borderline = 0
+    for q, d in enumerate(ds):
+        s = _single(d)
+        s.ps.initialize_particle_system()
+        sc, sl = s.ps.neighbors()
+        sid = s.ps.field("id0").cpu().numpy()
+        soff = np.concatenate([[0], np.cumsum(sc)])
+        lo = int(batch.offsets[q])
+        x = batch.scenes[q].x
+        R = s.ps.support_radius
+        for k in range(sid.size):
+            mine = set((sid[sl[soff[k]:soff[k + 1]]]).tolist())
+            kb = pos_b[int(sid[k]) + lo]
+            theirs = set((gid[lst[off[kb]:off[kb + 1]]] - lo).tolist())
+            for j in mine ^ theirs:
+                r = np.linalg.norm(x[sid[k]] - x[j])
+                assert abs(r - R) < 1e-6 * R, f"scene {q} pair ({sid[k]}, {j}) at r = {r}"
+                borderline += 1
+    assert borderline <= 8
+
+
+def test_batch_scene_vs_oracle(oracle_lib, native):
+    from tisphi_gb300.batch import SceneBatch
+    ds = _scenes()
+    batch = SceneBatch(ds)
+    batch.step(10)
+    for q in (0, 2):
+        orc = oracle_lib.OracleSim(cfg_of(ds[q]))
+        orc.step(10)
+        ids = orc.get("id0").astype(np.int64)
+        f = orc.get("mat_type") == 1
+        rho_o = np.empty_like(orc.get("density"))
+        rho_o[ids] = orc.get("density")
+        x_o = np.empty_like(orc.get("x"))
+        x_o[ids] = orc.get("x")
+        mt = np.empty_like(orc.get("mat_type"))
+        mt[ids] = orc.get("mat_type")
+        f = mt == 1
+        rho_b = batch.scene_field("density", q)
+        assert np.max(np.abs(rho_b[f] - rho_o[f]) / rho_o[f]) < 1e-5
+        assert np.max(np.abs(batch.scene_field("x", q)[f] - x_o[f])) < 1e-6
+
+
+def test_graph_replay_equals_eager(native):
+    from tisphi_gb300 import _native as nat
+    lib = nat.load()
+    d = small_dambreak_2d()
+    a, b = _single(d), _single(d)
+    a.solver.step(12)           # graph replays
+    lib.tsg_profile(1)          # per-phase events: eager steps
+    try:
+        b.solver.step(12)
+    finally:
+        ms = (ctypes.c_double * 16)()
+        cnt = (ctypes.c_int64 * 16)()
+        lib.tsg_profile_read(ms, cnt, len(nat.PHASES))
+        lib.tsg_profile(0)
+    for nm in ("x", "v", "density", "pressure", "id0"):
+        np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy(), err_msg=nm)
+
+
+@pytest.mark.parametrize("tpb", [64, 256])
+def test_threads_per_block_bit_identical(native, tpb):
+    from tisphi_gb300 import _native as nat
+    lib = nat.load()
+    d = small_dambreak_2d()
+    a, b = _single(d), _single(d)
+    cfg = nat.tsg_launch_cfg(tpb, 0, 4)
+    nat.check(lib.tsg_set_launch(b.ps._h, ctypes.byref(cfg)), "set_launch")
+    a.solver.step(9)
+    b.solver.step(9)
+    for nm in ("x", "v", "density"):
+        np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy(), err_msg=nm)
+
+
+@pytest.mark.parametrize("cpc", [2, 4, 8])
+def test_cells_per_cta_close(native, cpc):
+    from tisphi_gb300 import _native as nat
+    lib = nat.load()
+    d = small_dambreak_2d()
+    a, b = _single(d), _single(d)
+    cfg = nat.tsg_launch_cfg(128, cpc, 1)
+    nat.check(lib.tsg_set_launch(b.ps._h, ctypes.byref(cfg)), "set_launch")
+    a.solver.step(10)
+    b.solver.step(10)
+    f = _by_id0(a.ps, "mat_type") == 1
+    ra, rb = _by_id0(a.ps, "density")[f], _by_id0(b.ps, "density")[f]
+    assert np.max(np.abs(ra - rb) / ra) < 1e-6
+    assert np.max(np.abs(_by_id0(a.ps, "x") - _by_id0(b.ps, "x"))) < 1e-7
+
+
+def test_autotune_restores_state(native):
+    from tisphi_gb300.batch import SceneBatch
+    batch = SceneBatch(_scenes())
+    batch.step(5)
+    before = {q: {nm: batch.scene_field(nm, q) for nm in ("x", "v", "density")} for q in range(batch.nscenes)}
+    best = batch.autotune(trial_steps=4)
+    assert best["threads_per_block"] in (64, 128, 256) and best["ms_per_step"] > 0
+    assert best == {**batch.get_launch(), "ms_per_step": best["ms_per_step"]}
+    for q in range(batch.nscenes):
+        for nm, a in before[q].items():
+            np.testing.assert_array_equal(batch.scene_field(nm, q), a, err_msg=f"scene {q} {nm}")
+    batch.step(3)
+    batch.check_errors()

@@ -1,0 +1,128 @@
+"""Long rollouts: the FP64 GPU form against the f64 oracle, and the FP32-mixed form against
+the FP64 form, on conservation figures and on the dambreak front.
+
+* FP64 vs oracle: the full 2D water dambreak (9,144 particles, leap-frog at dt 1e-4) for
+  2,000 steps, and the two granular columns (mu(I), Drucker-Prager; 0.2 x 0.1 m at
+  spacing 0.002 m, 6,218 particles, symplectic Euler at dt 1e-5) for 1,000 steps: every
+  field bit-identical after the last step, so mass, momentum, energy and the front /
+  runout agree up to the summation order of the device reduction (rtol 1e-12).
+* FP32-mixed vs FP64, same 2,000-step dambreak: total mass identical within each form
+  (mass is never updated; drift exactly 0); the change of momentum and of mechanical
+  energy over the run within 1 % of the FP64 change; the front (largest fluid x) within
+  one particle spacing of the FP64 front; the final density field within 1e-3 RMS
+  relative error and 1e-2 max relative error (tolerances for a 2,000-step free-surface
+  flow, where single-step differences of 1e-7 grow through the splash).
+* FP32-mixed vs FP64, granular columns (mu(I), Drucker-Prager; spacing 0.002 m) for 2,000
+  steps: runout (largest soil x) within 0.1 particle spacing of the FP64 runout, and the
+  mean accumulated equivalent strain within 1 % of the FP64 mean.
+"""
+import numpy as np
+import pytest
+
+from helpers import cfg_of, describe_diff, small_column
+
+pytestmark = pytest.mark.gpu
+
+
+def _fields_equal(sim, orc, names):
+    bad = []
+    for nm in names:
+        a = sim.ps.field(nm).detach().cpu().numpy().astype(np.float64)
+        b = orc.get(nm)
+        same = (a == b) | (np.isnan(a) & np.isnan(b))
+        if not np.all(same):
+            bad.append(describe_diff(nm, a, b))
+    return bad
+
+
+def _oracle_diag(orc, gravity):
+    """The conservation figures of tsg_reduce_diag, from the oracle's f64 fields."""
+    mt = orc.get("mat_type").astype(np.int64)
+    flow = (mt == 1) | (mt == 2)
+    m, v, x = orc.get("mass")[flow], orc.get("v")[flow], orc.get("x")[flow]
+    return {"mass": m.sum(), "momentum": (m[:, None] * v).sum(0), "kinetic": 0.5 * (m * (v * v).sum(1)).sum(),
+            "potential": -(m * (x @ np.asarray(gravity, dtype=np.float64))).sum(),
+            "vmax": np.sqrt((v * v).sum(1)).max(), "front": x[:, 0].max()}
+
+
+def _diag_close(d_gpu, d_orc):
+    """Keys whose values differ beyond the summation-order rounding of a parallel reduction."""
+    bad = {}
+    for k in ("mass", "kinetic", "potential", "vmax", "front"):
+        if not np.isclose(d_gpu[k], d_orc[k], rtol=1e-12, atol=0.0):
+            bad[k] = (d_gpu[k], d_orc[k])
+    return bad
+
+
+def test_dambreak_2d_2000_steps_fp64_bit_exact(oracle_lib, native):
+    from tisphi_gb300 import scenes
+    from tisphi_gb300.simulation import Simulation
+    cfg = cfg_of(scenes.dambreak_2d())
+    sim = Simulation(cfg, precision="fp64")
+    orc = oracle_lib.OracleSim(cfg)
+    for _ in range(4):
+        sim.solver.step(500)
+        orc.step(500)
+    bad = _fields_equal(sim, orc, ["x", "v", "density", "pressure", "m_V", "id0"])
+    assert not bad, "after 2000 steps: " + "; ".join(bad)
+    assert not _diag_close(sim.ps.diagnostics(), _oracle_diag(orc, cfg.get_cfg("gravitation")))
+
+
+@pytest.mark.parametrize("method", [2, 3])
+def test_column_1000_steps_fp64_bit_exact(oracle_lib, native, method):
+    from tisphi_gb300.simulation import Simulation
+    cfg = cfg_of(small_column(method, spacing=0.002))
+    sim = Simulation(cfg, precision="fp64")
+    orc = oracle_lib.OracleSim(cfg)
+    sim.solver.step(1000)
+    orc.step(1000)
+    bad = _fields_equal(sim, orc, ["x", "v", "density", "pressure", "stress", "strain_equ", "id0"])
+    assert not bad, f"method {method} after 1000 steps: " + "; ".join(bad)
+    assert not _diag_close(sim.ps.diagnostics(), _oracle_diag(orc, cfg.get_cfg("gravitation")))
+
+
+def test_dambreak_2d_2000_steps_fp32_mixed_vs_fp64(native):
+    import torch
+
+    from tisphi_gb300 import compare, scenes
+    from tisphi_gb300.simulation import Simulation
+    cfg = cfg_of(scenes.dambreak_2d())
+    sims = {p: Simulation(cfg, precision=p) for p in ("fp32_mixed", "fp64")}
+    d0 = {p: s.ps.diagnostics() for p, s in sims.items()}
+    for s in sims.values():
+        s.solver.step(2000)
+    torch.cuda.synchronize()
+    dr = {p: compare.drift(d0[p], s.ps.diagnostics()) for p, s in sims.items()}
+    err = compare.field_errors(sims["fp32_mixed"].ps, sims["fp64"].ps, fields=("density", "x"))
+    report = f"drift {dr}, errors {err}"
+    for p in sims:
+        assert dr[p]["mass_rel"] == 0.0, report
+    m32, m64 = np.array(dr["fp32_mixed"]["momentum"]), np.array(dr["fp64"]["momentum"])
+    assert np.linalg.norm(m32 - m64) <= 1e-2 * np.linalg.norm(m64), report
+    e32, e64 = dr["fp32_mixed"]["energy"], dr["fp64"]["energy"]
+    assert abs(e32 - e64) <= 1e-2 * abs(e64), report
+    assert abs(dr["fp32_mixed"]["front"] - dr["fp64"]["front"]) <= 0.01, report  # one spacing
+    assert err["density"]["rms_rel"] <= 1e-3 and err["density"]["max_rel"] <= 1e-2, report
+
+
+@pytest.mark.parametrize("method", [2, 3])
+def test_column_2000_steps_fp32_mixed_vs_fp64(native, method):
+    import torch
+
+    from tisphi_gb300 import compare
+    from tisphi_gb300.simulation import Simulation
+    cfg = cfg_of(small_column(method, spacing=0.002))
+    sims = {p: Simulation(cfg, precision=p) for p in ("fp32_mixed", "fp64")}
+    d0 = {p: s.ps.diagnostics() for p, s in sims.items()}
+    for s in sims.values():
+        s.solver.step(2000)
+    torch.cuda.synchronize()
+    dr = {p: compare.drift(d0[p], s.ps.diagnostics()) for p, s in sims.items()}
+    eq = {}
+    for p, s in sims.items():
+        mt = s.ps.field("mat_type").cpu().numpy()
+        eq[p] = float(s.ps.field("strain_equ").cpu().numpy()[mt == 2].mean())
+    err = compare.field_errors(sims["fp32_mixed"].ps, sims["fp64"].ps, fields=("density", "x", "stress"))
+    report = f"method {method}: drift {dr}, mean strain_equ {eq}, errors {err}"
+    assert abs(dr["fp32_mixed"]["front"] - dr["fp64"]["front"]) <= 0.1 * 0.002, report
+    assert abs(eq["fp32_mixed"] - eq["fp64"]) <= 1e-2 * abs(eq["fp64"]), report

@@ -46,6 +46,11 @@ class tsg_particles(ctypes.Structure):
                 ("is_dynamic", _ip)]
 
 
+class tsg_launch_cfg(ctypes.Structure):
+    _fields_ = [("threads_per_block", ctypes.c_int32), ("cells_per_cta", ctypes.c_int32),
+                ("steps_per_graph", ctypes.c_int32)]
+
+
 class tsg_view(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("dtype", ctypes.c_int32), ("ndim", ctypes.c_int32),
                 ("shape", ctypes.c_int64 * 3), ("strides", ctypes.c_int64 * 3)]
@@ -67,7 +72,15 @@ SYMBOLS = {
     "tsg_neighbors": (ctypes.c_int, [ctypes.c_void_p, _ip, _ip, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64),
                                      ctypes.c_void_p]),
     "tsg_reduce_diag": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
+    "tsg_list_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p]),
     "tsg_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "tsg_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "tsg_get_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "tsg_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, _dp, ctypes.c_void_p]),
+    "tsg_batch_create": (ctypes.c_int, [ctypes.POINTER(tsg_config), ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "tsg_batch_diag": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int32, ctypes.c_void_p]),
+    "tsg_batch_pitch": (ctypes.c_double, [ctypes.c_void_p]),
     "tsg_write": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "tsg_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "tsg_launch_count": (ctypes.c_int64, []),

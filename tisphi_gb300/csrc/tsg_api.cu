@@ -17,6 +17,8 @@ using namespace tsg;
 namespace tsg {
 static std::atomic<long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void add_launches(long long delta) { g_launches.fetch_add(delta, std::memory_order_relaxed); }
+long long launch_total() { return g_launches.load(std::memory_order_relaxed); }
 
 struct ProfRec { int phase; cudaEvent_t a, b; };
 struct Profiler {
@@ -29,6 +31,7 @@ struct Profiler {
     }
 };
 static Profiler g_prof;
+bool profiling_on() { return g_prof.on; }
 
 PhaseScope::PhaseScope(cudaStream_t s, int phase) : s_(s), phase_(phase), stop_(nullptr) {
     if (!g_prof.on) return;
@@ -56,6 +59,8 @@ struct tsg_handle {
     double* d_scratch = nullptr;    // small reductions
     std::vector<void*> allocs;
     Fp32State* f32 = nullptr;       // FP32-mixed form (nullptr for FP64)
+    int nscenes = 0;                // batched ensemble (tsg_batch_create): scenes and x pitch
+    double batch_pitch = 0.0;
 };
 
 namespace {
@@ -265,7 +270,22 @@ int tsg_create(const tsg_config* cfg, tsg_handle** out) {
     return 0;
 }
 
+}  // extern "C"
+
+namespace {
+int upload_impl(tsg_handle* h, const tsg_particles* p, int from_device, void* stream, const Fp32Scenes* scenes);
+}
+
+extern "C" {
+
 int tsg_upload(tsg_handle* h, const tsg_particles* p, int from_device, void* stream) {
+    return upload_impl(h, p, from_device, stream, nullptr);
+}
+
+}  // extern "C"
+
+namespace {
+int upload_impl(tsg_handle* h, const tsg_particles* p, int from_device, void* stream, const Fp32Scenes* scenes) {
     if (!h || !p || p->n <= 0 || p->n > (1ll << 30) || !p->x || !p->v || !p->density || !p->mass || !p->m_V ||
         !p->pressure || !p->mat_type || !p->mat_id || !p->obj_id || !p->is_dynamic)
         return TSG_E_ARG;
@@ -306,7 +326,7 @@ int tsg_upload(tsg_handle* h, const tsg_particles* p, int from_device, void* str
             if (xz[3 * i + 2] != 0.0 || vz[3 * i + 2] != 0.0) return TSG_E_UNSUPPORTED;
     }
     if (h->cfg.precision == TSG_FP32_MIXED) {
-        int rc = fp32_create(h->cfg, c, p, from_device != 0, &h->f32, s);
+        int rc = fp32_create(h->cfg, c, p, from_device != 0, &h->f32, s, scenes);
         if (rc) return rc;
         h->uploaded = true;
         return check_cuda();
@@ -332,6 +352,9 @@ int tsg_upload(tsg_handle* h, const tsg_particles* p, int from_device, void* str
     h->pos32_dirty = true;
     return check_cuda();
 }
+}  // namespace
+
+extern "C" {
 
 int64_t tsg_particle_num(const tsg_handle* h) { return h ? h->n : 0; }
 
@@ -420,6 +443,14 @@ int tsg_step(tsg_handle* h, int nsteps, void* stream) {
     if (!h || !h->uploaded) return TSG_E_STATE;
     if (nsteps < 0) return TSG_E_ARG;
     const bool collide = h->c.boundary == 1;
+    // FP32-mixed: replay captured step graphs (no host round trip per step) unless per-phase
+    // profiling wants its events, which the eager path below records
+    if (use_fp32(h) && !profiling_on() && nsteps > 0) {
+        int rc = fp32_step_graph(*h->f32, nsteps, collide, S(stream));
+        if (rc) return rc;
+        h->sorted = true;
+        return check_cuda();
+    }
     for (int k = 0; k < nsteps; ++k) {
         int rc;
         // FP32-mixed with a neighbour skin re-sorts only when its lists expire
@@ -630,6 +661,14 @@ int tsg_reduce_diag(tsg_handle* h, double out[8], void* stream) {
     return check_cuda();
 }
 
+int tsg_list_stats(tsg_handle* h, int64_t out[4], void* stream) {
+    if (!h || !out || !h->uploaded) return TSG_E_STATE;
+    if (!use_fp32(h)) return TSG_E_UNSUPPORTED;
+    int rc = fp32_list_stats(*h->f32, out, S(stream));
+    if (rc) return rc;
+    return check_cuda();
+}
+
 int tsg_last_error(tsg_handle* h, void* stream) {
     if (!h || !h->uploaded) return TSG_E_STATE;
     cudaStream_t s = S(stream);
@@ -641,6 +680,121 @@ int tsg_last_error(tsg_handle* h, void* stream) {
     int e = check_cuda();
     return e ? e : v;
 }
+
+int tsg_set_launch(tsg_handle* h, const tsg_launch_cfg* cfg) {
+    if (!h || !cfg) return TSG_E_ARG;
+    if (!use_fp32(h)) return TSG_E_UNSUPPORTED;
+    return fp32_set_launch(*h->f32, cfg->threads_per_block, cfg->cells_per_cta, cfg->steps_per_graph);
+}
+
+int tsg_get_launch(tsg_handle* h, tsg_launch_cfg* cfg) {
+    if (!h || !cfg) return TSG_E_ARG;
+    if (!use_fp32(h)) return TSG_E_UNSUPPORTED;
+    fp32_get_launch(*h->f32, &cfg->threads_per_block, &cfg->cells_per_cta, &cfg->steps_per_graph);
+    return 0;
+}
+
+int tsg_autotune(tsg_handle* h, int32_t trial_steps, tsg_launch_cfg* best, double* ms_per_step, void* stream) {
+    if (!h || !h->uploaded) return TSG_E_STATE;
+    if (!use_fp32(h)) return TSG_E_UNSUPPORTED;
+    float ms = 0.f;
+    int rc = fp32_autotune(*h->f32, trial_steps, h->c.boundary == 1, S(stream), &ms);
+    if (rc) return rc;
+    h->sorted = true;
+    if (best) fp32_get_launch(*h->f32, &best->threads_per_block, &best->cells_per_cta, &best->steps_per_graph);
+    if (ms_per_step) *ms_per_step = ms;
+    return check_cuda();
+}
+
+int tsg_batch_create(const tsg_config* cfgs, const tsg_particles* parts, int32_t nscenes, void* stream,
+                     tsg_handle** out) {
+    if (!cfgs || !parts || !out || nscenes <= 0) return TSG_E_ARG;
+    *out = nullptr;
+    if (nscenes > 4096) return TSG_E_CAPACITY;
+    const tsg_config& a = cfgs[0];
+    if (a.precision != TSG_FP32_MIXED || a.solver != 1 || a.boundary != 2) return TSG_E_UNSUPPORTED;
+    // every scene shares the geometry, the kernel and the integrator; stiffness and
+    // viscosity may differ per scene
+    for (int q = 1; q < nscenes; ++q) {
+        const tsg_config& b = cfgs[q];
+        bool same = b.dim == a.dim && b.solver == a.solver && b.kernel == a.kernel && b.kernel_corr == a.kernel_corr &&
+                    b.time_integration == a.time_integration && b.xsph == a.xsph && b.boundary == a.boundary &&
+                    b.precision == a.precision && b.exponent_is_int == a.exponent_is_int &&
+                    b.grid_num_total == a.grid_num_total && b.grid_size == a.grid_size &&
+                    b.support_radius == a.support_radius && b.smoothing_len == a.smoothing_len &&
+                    b.particle_diameter == a.particle_diameter && b.particle_radius == a.particle_radius &&
+                    b.dt == a.dt && b.density0 == a.density0 && b.exponent == a.exponent && b.list_skin == a.list_skin;
+        for (int d = 0; d < 3; ++d)
+            same = same && b.grid_num[d] == a.grid_num[d] && b.vdomain_start[d] == a.vdomain_start[d] &&
+                   b.domain_start[d] == a.domain_start[d] && b.domain_end[d] == a.domain_end[d] &&
+                   b.gravity[d] == a.gravity[d];
+        if (!same) return TSG_E_CONFIG;
+    }
+    // scenes side by side along x, two reference cells apart beyond their virtual domains:
+    // particles of different scenes are then farther apart than the support plus the skin
+    const int pitch_cells = a.grid_num[0] + 2;
+    const double pitch = pitch_cells * a.grid_size;
+    tsg_config t = a;
+    t.grid_num[0] = pitch_cells * nscenes;
+    t.grid_num_total = (int64_t)t.grid_num[0] * t.grid_num[1] * t.grid_num[2];
+    t.domain_end[0] = a.domain_end[0] + (nscenes - 1) * pitch;
+    if (t.grid_num_total > (1ll << 30)) return TSG_E_CAPACITY;
+    int64_t n = 0;
+    for (int q = 0; q < nscenes; ++q) {
+        const tsg_particles& p = parts[q];
+        if (p.n <= 0 || !p.x || !p.v || !p.density || !p.mass || !p.m_V || !p.pressure || !p.mat_type || !p.mat_id ||
+            !p.obj_id || !p.is_dynamic)
+            return TSG_E_ARG;
+        n += p.n;
+    }
+    if (n > (1ll << 30)) return TSG_E_CAPACITY;
+    std::vector<double> x(3 * n), v(3 * n), rho(n), mass(n), mV(n), pr(n);
+    std::vector<int32_t> mt(n), mid(n), oid(n), dyn(n), scene(n);
+    std::vector<float> stiff(nscenes), vfac(nscenes);
+    int64_t o = 0;
+    for (int q = 0; q < nscenes; ++q) {
+        const tsg_particles& p = parts[q];
+        for (int64_t i = 0; i < p.n; ++i, ++o) {
+            for (int d = 0; d < 3; ++d) {
+                x[3 * o + d] = p.x[3 * i + d] + (d == 0 ? q * pitch : 0.0);
+                v[3 * o + d] = p.v[3 * i + d];
+            }
+            rho[o] = p.density[i]; mass[o] = p.mass[i]; mV[o] = p.m_V[i]; pr[o] = p.pressure[i];
+            mt[o] = p.mat_type[i]; mid[o] = p.mat_id[i]; oid[o] = p.obj_id[i]; dyn[o] = p.is_dynamic[i];
+            scene[o] = q;
+        }
+        stiff[q] = (float)cfgs[q].stiffness;
+        vfac[q] = (float)(2 * (a.dim + 2) * cfgs[q].viscosity);
+    }
+    tsg_handle* h = nullptr;
+    int rc = tsg_create(&t, &h);
+    if (rc) return rc;
+    tsg_particles all{};
+    all.n = n;
+    all.x = x.data(); all.v = v.data(); all.density = rho.data(); all.mass = mass.data(); all.m_V = mV.data();
+    all.pressure = pr.data(); all.stress = nullptr;
+    all.mat_type = mt.data(); all.mat_id = mid.data(); all.obj_id = oid.data(); all.is_dynamic = dyn.data();
+    Fp32Scenes sc;
+    sc.scene_of = scene.data();
+    sc.stiffness = stiff.data();
+    sc.visc_fac = vfac.data();
+    sc.nscenes = nscenes;
+    rc = upload_impl(h, &all, 0, stream, &sc);
+    if (rc) { tsg_destroy(h); return rc; }
+    h->batch_pitch = pitch;
+    h->nscenes = nscenes;
+    *out = h;
+    return 0;
+}
+
+int tsg_batch_diag(tsg_handle* h, double* out, int32_t nscenes, void* stream) {
+    if (!h || !out || !h->uploaded) return TSG_E_STATE;
+    if (!use_fp32(h) || h->nscenes <= 0) return TSG_E_UNSUPPORTED;
+    int rc = fp32_batch_diag(*h->f32, h->batch_pitch, out, nscenes, S(stream));
+    return rc ? rc : check_cuda();
+}
+
+double tsg_batch_pitch(const tsg_handle* h) { return h ? h->batch_pitch : 0.0; }
 
 void tsg_destroy(tsg_handle* h) {
     if (!h) return;

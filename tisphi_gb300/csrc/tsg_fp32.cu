@@ -49,10 +49,20 @@ struct K32 {
     float R2L, R2Lhi, disp2_limit;  // list radius (support + skin) and rebuild threshold
     float visc_fac, eps_h2, rho0, B, gamma, dt, hdt, g[3], rep_fac, diam, h075, r_eps;
     float ds[3], de[3];
+    // granular solvers (mu(I): mu, c2, coh; Drucker-Prager: alpha ... twoG; both: damping)
+    float mu, c2, coh, alpha, k_c, kc_over_alpha, Gm, Km, sin_dila, lam_den, three_aK, nine_K_sin, twoG;
+    float damp_eps, damp_E, h2;
+    // batched ensembles: per-scene (stiffness B, viscosity factor), indexed by the scene
+    // number in the type word; nullptr for a single scene (B and visc_fac above)
+    const float2* scene_par;
 };
 
+// Type word (the w lane of lo): bits 0-15 material type (signed), bit 16 is_dynamic, bits
+// 17-28 scene number of a batched ensemble, bit 30 set (the word stays a normal float).
 __device__ __forceinline__ int tf_type(float w) { return (int)(short)(__float_as_int(w) & 0xffff); }
 __device__ __forceinline__ int tf_dyn(float w) { return (__float_as_int(w) >> 16) & 1; }
+__device__ __forceinline__ int tf_scene(float w) { return (__float_as_int(w) >> 17) & 0xfff; }
+constexpr int kMaxScenes = 4096;
 __device__ __forceinline__ bool is_flow(int t) { return t == MAT_FLUID || t == MAT_SOIL; }
 
 // Block-compensated accumulator: plain partial sums, Kahan-folded every flush.
@@ -69,12 +79,24 @@ struct CSum {
     __device__ __forceinline__ float get() { flush(); return s; }
 };
 
+__device__ __forceinline__ void atomic_max_d(double* addr, double v) {
+    unsigned long long* a = reinterpret_cast<unsigned long long*>(addr);
+    unsigned long long old = *a;
+    while (__longlong_as_double(old) < v) {
+        unsigned long long prev = atomicCAS(a, old, __double_as_longlong(v));
+        if (prev == old) break;
+        old = prev;
+    }
+}
+
 // Cell coordinate trunc((hi + lo) / grid) with the f64 semantics of the reference's cast:
-// an f32 estimate decides unless it lies within 1e-3 of an integer, where f64 decides.
+// an f32 estimate decides unless it lies within its error bound (1e-3 + |t| 2^-20, well
+// above the three roundings of the f32 estimate) of an integer, where f64 decides.
 __device__ __forceinline__ long long cell_coord(const K32& k, float hi, float lo, bool& ok) {
     const float tf = (hi + lo) * k.inv_grid;
-    const float fr = tf - truncf(tf);
-    if (fabsf(tf) < 1.0e6f && fabsf(fr) > 1e-3f && fabsf(fr) < 0.999f) return (long long)(int)tf;
+    const float fr = fabsf(tf - truncf(tf));
+    const float margin = 1e-3f + fabsf(tf) * 9.5367431640625e-7f;
+    if (fabsf(tf) < 1.0e6f && fr > margin && fr < 1.f - margin) return (long long)(int)tf;
     const double t = ((double)hi + (double)lo) / k.grid;
     if (!(fabs(t) < 2147483647.0)) { ok = false; return 0; }
     return (long long)(int)t;
@@ -120,21 +142,26 @@ __device__ __forceinline__ void delta(const float4& hi_i, const float4& lo_i, co
 
 // Candidate enumeration over the stencil of i (reference traversal order of cells, dynamic
 // block first, then the static block for flow centres).  body(j, d, r2) gets the exact
-// f32 displacement x_i - x_j.
+// f32 displacement x_i - x_j.  The cheap prefilter compares the positions of the last list
+// build (PF): with a skin, particles have moved at most 0.45 skin since then while the
+// lists are in use, so a build-time distance above (R + skin)(1 + 2^-11) rules a pair out
+// for the current positions as well.  Callers after advect_pos (positions moved past the
+// last check) pass use_pf = false.
 template <int DIM, class F>
 __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4* __restrict__ HI,
                                                const float4* __restrict__ LO, const float4* __restrict__ PF,
                                                const int* __restrict__ dstart, const int* __restrict__ sstart,
-                                               bool flow_i, F&& body, bool list_radius = false) {
+                                               bool flow_i, F&& body, bool list_radius = false,
+                                               bool use_pf = true) {
     const float cut2 = list_radius ? k.R2L : k.R2;
-    const float cut2hi = list_radius ? k.R2Lhi : k.R2hi;
+    const float cut2hi = k.R2Lhi;
     const float4 hi_i = HI[i], lo_i = LO[i], pf_i = PF[i];
     bool ok = true;
     const long long cc0 = cell_coord(k, hi_i.x, lo_i.x, ok);
     const long long cc1 = cell_coord(k, hi_i.y, lo_i.y, ok);
     const long long cc2 = cell_coord(k, hi_i.z, lo_i.z, ok);
     if (!ok) return;
-    const bool pf = fabsf(pf_i.x) < k.pf_lim && fabsf(pf_i.y) < k.pf_lim && fabsf(pf_i.z) < k.pf_lim;
+    const bool pf = use_pf && fabsf(pf_i.x) < k.pf_lim && fabsf(pf_i.y) < k.pf_lim && fabsf(pf_i.z) < k.pf_lim;
     const long long ny = k.gnum[1], nz = k.gnum[2], G = k.G;
     for (int blk = 0; blk < (flow_i ? 2 : 1); ++blk) {
         const int* cs = blk == 0 ? dstart : sstart;
@@ -281,7 +308,15 @@ struct P32 {
     float* drho;    // density - rho0
     float* mass;
     int4* ids;      // (id0, mat_id, obj_id, is_dynamic)
+    // granular solvers only (nullptr for WCSPH)
+    float* sig;     // stress, 6 planes of n (symmetric: xx, yy, zz, xy, xz, yz)
+    float* eeq;     // equivalent strain
+    float* eeqp;    // equivalent plastic strain (Drucker-Prager)
+    int* flag;      // return-mapping case (Drucker-Prager)
 };
+
+// Symmetric 3x3 tensors are stored as six planes: xx, yy, zz, xy, xz, yz.
+__device__ __forceinline__ int sym_idx(int a, int b) { return a == b ? a : 2 + a + b; }
 
 // Gather block [base, base + count_n) from a into b (new order), renormalise hi/lo and
 // refresh the prefilter position.
@@ -306,6 +341,13 @@ __global__ void k_reorder32(K32 k, int count_n, int base, const int* __restrict_
     b.drho[dst] = a.drho[src];
     b.mass[dst] = a.mass[src];
     b.ids[dst] = a.ids[src];
+    if (a.sig) {
+        const size_t n = k.n;
+        for (int q = 0; q < 6; ++q) b.sig[q * n + dst] = a.sig[q * n + src];
+        b.eeq[dst] = a.eeq[src];
+        b.eeqp[dst] = a.eeqp[src];
+        b.flag[dst] = a.flag[src];
+    }
     PF[dst] = make_float4(pfv[0], pfv[1], pfv[2], l.w);
 }
 
@@ -336,18 +378,18 @@ __global__ void k_lists(K32 k, const float4* __restrict__ HI, const float4* __re
 // coalesced loads and tested by every lane from a broadcast read.  Lanes whose particle
 // sits in an aliased cell (true cell coordinates outside the grid) and particles in the
 // out-of-grid bin take the per-particle path.
-template <int DIM>
+template <int DIM, int WPB>
 __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells, const int* __restrict__ cell_count,
                              const float4* __restrict__ HI, const float4* __restrict__ LO,
                              const float4* __restrict__ PF, const int* __restrict__ dstart,
                              const int* __restrict__ sstart, int* __restrict__ cnt, int* __restrict__ nbr,
                              int* __restrict__ ovf_list, int* __restrict__ novf) {
-    __shared__ float4 sh_rel[4][32];
+    __shared__ float4 sh_rel[WPB][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int* own = self_blk == 0 ? dstart : sstart;
     const int ncell = *cell_count;
     const long long ny = k.gnum[1], nz = k.gnum[2], G = k.G;
-    for (int w = blockIdx.x * 4 + wib; w < ncell; w += gridDim.x * 4) {
+    for (int w = blockIdx.x * WPB + wib; w < ncell; w += gridDim.x * WPB) {
     const long long c = cells[w];
     const int cb = own[c], ce = own[c + 1];
     const long long cx = c / (ny * nz), cy = (c / nz) % ny, cz = c % nz;
@@ -495,6 +537,11 @@ struct T32 {
     float4* xs;     // XSPH sums
     int* cnt;
     int* nbr;
+    // granular solvers only
+    float* sigt;    // stress_tmp, 6 planes
+    float* dsig;    // d_stress, 6 planes (Drucker-Prager)
+    float* dee;     // d_strain_equ
+    float* deep;    // d_strain_equ_p (Drucker-Prager)
 };
 
 template <int DIM>
@@ -557,16 +604,21 @@ __global__ void k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, con
 __global__ void k_init_tmp32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
-    if (tf_type(p.lo[i].w) > 0) {
+    const int ti = tf_type(p.lo[i].w);
+    if (ti > 0) {
         const float4 v = p.vel[i];
         t.vt[i] = make_float4(v.x, v.y, v.z, t.vt[i].w);
         t.drt[i] = p.drho[i];
+    }
+    if (ti == MAT_SOIL && t.sigt) {
+        const size_t n = k.n;
+        for (int q = 0; q < 6; ++q) t.sigt[q * n + i] = p.sig[q * n + i];
     }
 }
 
 // Tait EOS from the density deviation e = (rho_tmp - rho0) / rho0:
 // (1 + e)^g - 1 = e * sum_{k<g} (1 + e)^k for an integer exponent (no cancellation).
-__device__ __forceinline__ float tait(const K32& k, float drt) {
+__device__ __forceinline__ float tait(const K32& k, float drt, float B) {
     const float e = drt / k.rho0;
     float r;
     if (k.exponent_is_int && k.gamma_i >= 1) {
@@ -577,15 +629,16 @@ __device__ __forceinline__ float tait(const K32& k, float drt) {
     } else {
         r = expm1f(k.gamma * log1pf(e));
     }
-    return fmaxf(k.B * r, 0.f);
+    return fmaxf(B * r, 0.f);
 }
 
 __global__ void k_pre32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    if (tf_type(p.lo[i].w) != MAT_FLUID) return;
+    const float w = p.lo[i].w;
+    if (tf_type(w) != MAT_FLUID) return;
     const float drt = t.drt[i];
-    const float pr = tait(k, drt);
+    const float pr = tait(k, drt, k.scene_par ? k.scene_par[tf_scene(w)].x : k.B);
     const float rt = k.rho0 + drt;
     p.vel[i].w = pr;
     t.vt[i].w = pr / (rt * rt);
@@ -634,7 +687,9 @@ template <int DIM, bool FB, bool CORR>
 __global__ void k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                           const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
-      if (tf_type(p.lo[i].w) == MAT_FLUID) {
+      const float wi = p.lo[i].w;
+      if (tf_type(wi) == MAT_FLUID) {
+        const float visc_fac = k.scene_par ? k.scene_par[tf_scene(wi)].y : k.visc_fac;
         const float4 vti = t.vt[i];
         const float rti = k.rho0 + t.drt[i];
         const float visc_b = k.rho0 / rti;
@@ -665,7 +720,7 @@ __global__ void k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, co
             const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
             // WCSPH scenes hold fluid, dummy, repulsive and rigid particles only (soil is rejected
             // at upload), so every non-fluid neighbour takes the boundary form
-            const float cv = __fdividef(k.visc_fac * hj.w * fminf(vdx, 0.f), r2 + k.eps_h2) *
+            const float cv = __fdividef(visc_fac * hj.w * fminf(vdx, 0.f), r2 + k.eps_h2) *
                              (tj == MAT_FLUID ? 1.f : visc_b);
             const float cp = -k.rho0 * hj.w * (vti.w + vtj.w);
             float sc = (cv + cp) * gf;
@@ -692,11 +747,362 @@ __global__ void k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, co
     });
 }
 
+// ---------------------------------------------------------------- granular solvers
+// Drucker-Prager invariants and stress adaptation (eng/solver_sph_dp.py:42-109) on the
+// six stored components; s:s counts each off-diagonal entry twice.
+__device__ __forceinline__ void dp_inv32(const K32& k, const float* st, float* s, float& I1, float& sJ2, float& f) {
+    const float tr = (st[0] + st[1]) + st[2];
+    const float t3 = tr / 3.f;
+    s[0] = st[0] - t3; s[1] = st[1] - t3; s[2] = st[2] - t3;
+    s[3] = st[3]; s[4] = st[4]; s[5] = st[5];
+    I1 = tr;
+    const float ss = s[0] * s[0] + s[1] * s[1] + s[2] * s[2] + 2.f * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
+    sJ2 = sqrtf(0.5f * ss);
+    f = sJ2 + k.alpha * I1 - k.k_c;
+}
+__device__ __forceinline__ void dp_adapt32(const K32& k, float* st) {
+    float s[6], I1, sJ2, f;
+    dp_inv32(k, st, s, I1, sJ2, f);
+    if (f > (float)EPS_F) {
+        if (f > sJ2) {
+            const float tt = (I1 - k.kc_over_alpha) / 3.f;
+            st[0] -= tt; st[1] -= tt; st[2] -= tt;
+        }
+        dp_inv32(k, st, s, I1, sJ2, f);
+        const float r = (-I1 * k.alpha + k.k_c) / sJ2;
+        for (int q = 0; q < 6; ++q) st[q] = r * s[q] + (q < 3 ? I1 / 3.f : 0.f);
+    }
+}
+__device__ __forceinline__ int dp_flag32(const K32& k, const float* st) {
+    float s[6], I1, sJ2, f;
+    dp_inv32(k, st, s, I1, sJ2, f);
+    if (f < -(float)EPS_F) return 0;
+    if (f > (float)EPS_F) return f >= sJ2 ? 3 : 2;
+    return 1;
+}
+
+__device__ __forceinline__ void load_sym(const float* __restrict__ a, size_t n, int i, float* out) {
+    for (int q = 0; q < 6; ++q) out[q] = a[q * n + i];
+}
+__device__ __forceinline__ void store_sym(float* __restrict__ a, size_t n, int i, const float* v) {
+    for (int q = 0; q < 6; ++q) a[q * n + i] = v[q];
+}
+
+// Drucker-Prager first phase of one_step: adapt stress_tmp (eng/solver_sph_dp.py:215-217).
+__global__ void k_pre_dp32(K32 k, P32 p, T32 t) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd) return;
+    if (tf_type(p.lo[i].w) != MAT_SOIL) return;
+    float st[6];
+    load_sym(t.sigt, k.n, i, st);
+    dp_adapt32(k, st);
+    store_sym(t.sigt, k.n, i, st);
+}
+
+// Corrected kernel gradient L (G d) (or G d when CORR is off).
+template <int DIM, bool CORR>
+__device__ __forceinline__ void grad_c(const float* L, float gf, const float* d, float* kc) {
+    const float gx = gf * d[0], gy = gf * d[1], gz = DIM == 3 ? gf * d[2] : 0.f;
+    if (CORR) {
+        kc[0] = L[0] * gx + L[1] * gy + (DIM == 3 ? L[2] * gz : 0.f);
+        kc[1] = L[3] * gx + L[4] * gy + (DIM == 3 ? L[5] * gz : 0.f);
+        kc[2] = DIM == 3 ? L[6] * gx + L[7] * gy + L[8] * gz : 0.f;
+    } else {
+        kc[0] = gx; kc[1] = gy; kc[2] = gz;
+    }
+}
+
+// Velocity gradient sum_j m_Vj (v_j - v_i) (x) kc and continuity sum_j m_Vj (v_i - v_j) . kc.
+template <int DIM>
+__device__ __forceinline__ void vgrad_add(float mVj, const float4& vti, const float4& vtj, const float* kc, float* vg,
+                                          CSum& dd) {
+    const float u[3] = {mVj * (vtj.x - vti.x), mVj * (vtj.y - vti.y), DIM == 3 ? mVj * (vtj.z - vti.z) : 0.f};
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+#pragma unroll
+        for (int b = 0; b < DIM; ++b) vg[3 * a + b] += u[a] * kc[b];
+    dd.add(-(u[0] * kc[0] + u[1] * kc[1] + (DIM == 3 ? u[2] * kc[2] : 0.f)));
+}
+
+// Symmetric / antisymmetric parts of a full velocity gradient.
+__device__ __forceinline__ void strain_rate(const float* vg, float* er) {
+    er[0] = vg[0]; er[1] = vg[4]; er[2] = vg[8];
+    er[3] = 0.5f * (vg[1] + vg[3]); er[4] = 0.5f * (vg[2] + vg[6]); er[5] = 0.5f * (vg[5] + vg[7]);
+}
+__device__ __forceinline__ float sym_dd(const float* a, const float* b) {
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + 2.f * (a[3] * b[3] + a[4] * b[4] + a[5] * b[5]);
+}
+__device__ __forceinline__ float equiv_rate(const float* er) {  // sqrt(2/3 dev(e):dev(e))
+    const float t3 = ((er[0] + er[1]) + er[2]) / 3.f;
+    float ed[6] = {er[0] - t3, er[1] - t3, er[2] - t3, er[3], er[4], er[5]};
+    return sqrtf(sym_dd(ed, ed) * 2.f / 3.f);
+}
+
+// mu(I) loop 1 (eng/solver_sph_muI.py:67-92): velocity gradient, continuity, pressure from
+// density (not density_tmp), mu(I) stress, equivalent strain rate.
+template <int DIM, bool FB, bool CORR>
+__global__ void k_mui_stress32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
+                               const int* __restrict__ sstart, Ovf ovf) {
+    FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
+      if (tf_type(p.lo[i].w) == MAT_SOIL) {
+        const float4 vti = t.vt[i];
+        float L[9];
+        if (CORR)
+            for (int q = 0; q < 9; ++q) L[q] = t.L[(size_t)q * k.n + i];
+        float vg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        CSum dd;
+        for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
+                          [&](int j, const float* d, float r2, int sidx) {
+            float kc[3];
+            grad_c<DIM, CORR>(L, w_grad(k, fast_sqrt(r2)), d, kc);
+            vgrad_add<DIM>(p.hi[j].w, vti, t.vt[j], kc, vg, dd);
+            if ((sidx & 7) == 7) dd.flush();
+        });
+        const size_t n = k.n;
+        t.dd[i] = dd.get() * (k.rho0 + t.drt[i]);
+        const float pr = fmaxf(k.c2 * p.drho[i], 0.f);
+        p.vel[i].w = pr;
+        float er[6];
+        strain_rate(vg, er);
+        const float dbdot = sqrtf(0.5f * sym_dd(er, er)) + (float)EPS;
+        const float sc = (k.coh + pr * k.mu) / dbdot;
+        for (int q = 0; q < 6; ++q) t.sigt[q * n + i] = sc * er[q] - (q < 3 ? pr : 0.f);
+        t.dee[i] = equiv_rate(er);
+      }
+    });
+}
+
+// Boundary extrapolation for the granular solvers (eng/solver_sph_muI.py:97-109,
+// eng/solver_sph_dp.py:219-234): velocity, density (mu(I)) and stress with the
+// hydrostatic correction rho_j g_a (x_i - x_j)_a on the diagonal.
+template <int DIM, bool FB>
+__global__ void k_bdy_soil32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
+                             const int* __restrict__ sstart, int base, int count_n, Ovf ovf) {
+    const int lim = base + count_n;
+    FOR_PARTICLES(FB, base, lim, ovf, t.cnt, k.maxn, {
+        const int ti = tf_type(p.lo[i].w);
+        if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
+            const size_t n = k.n;
+            CSum bv[3], b1, b2;
+            float bs[6] = {0, 0, 0, 0, 0, 0};
+            for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
+                              [&](int j, const float* d, float r2, int sidx) {
+                const float mw = p.hi[j].w * w_val(k, fast_sqrt(r2));
+                const float4 vt = t.vt[j];
+                const float drt = t.drt[j];
+                const float rtj = k.rho0 + drt;
+                bv[0].add(mw * vt.x);
+                bv[1].add(mw * vt.y);
+                if (DIM == 3) bv[2].add(mw * vt.z);
+                if (k.solver == 2) { b1.add(mw); b2.add(mw * drt); }
+                bs[0] += mw * (t.sigt[j] + rtj * k.g[0] * d[0]);
+                bs[1] += mw * (t.sigt[n + j] + rtj * k.g[1] * d[1]);
+                bs[2] += mw * (t.sigt[2 * n + j] + (DIM == 3 ? rtj * k.g[2] * d[2] : 0.f));
+                bs[3] += mw * t.sigt[3 * n + j];
+                if (DIM == 3) { bs[4] += mw * t.sigt[4 * n + j]; bs[5] += mw * t.sigt[5 * n + j]; }
+                if ((sidx & 7) == 7) { bv[0].flush(); bv[1].flush(); bv[2].flush(); b1.flush(); b2.flush(); }
+            });
+            const float f = t.cf[i];
+            const float4 v = p.vel[i];
+            const float b0 = bv[0].get(), b1v = bv[1].get(), b2v = DIM == 3 ? bv[2].get() : 0.f;
+            t.vt[i] = make_float4(2.f * v.x - b0 * f, 2.f * v.y - b1v * f, 2.f * v.z - b2v * f, 0.f);
+            // max(f sum m_V rho_tmp W, rho0) - rho0, with rho_tmp = rho0 + drt split off exactly
+            t.drt[i] = k.solver == 2 ? fmaxf(k.rho0 * (f * b1.get() - 1.f) + f * b2.get(), 0.f) : 0.f;
+            for (int q = 0; q < 6; ++q) t.sigt[q * n + i] = bs[q] * f;
+            if (ti == MAT_RIGID) { t.dd[i] = 0.f; t.dv[i] = make_float4(0.f, 0.f, 0.f, 0.f); }
+        }
+    });
+}
+
+// Stress divergence + damping (mu(I), eng/solver_sph_muI.py:113-128), and for DP also the
+// velocity gradient, continuity and Bui-2008 stress rate (eng/solver_sph_dp.py:172-208,
+// :236-270), all in one traversal.
+template <int DIM, bool FB, bool CORR, bool DP>
+__global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
+                             const int* __restrict__ sstart, Ovf ovf) {
+    FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
+      if (tf_type(p.lo[i].w) == MAT_SOIL) {
+        const size_t n = k.n;
+        const float4 vti = t.vt[i];
+        float L[9];
+        if (CORR)
+            for (int q = 0; q < 9; ++q) L[q] = t.L[(size_t)q * n + i];
+        float sti[6];
+        load_sym(t.sigt, n, i, sti);
+        const float rti = k.rho0 + t.drt[i];
+        const float ir2 = 1.f / (rti * rti);
+        float ai[6];
+        for (int q = 0; q < 6; ++q) ai[q] = sti[q] * ir2;
+        CSum dv[3], dd;
+        float vg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const bool rep_on = k.boundary == 3 || k.boundary == 4;
+        for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
+                          [&](int j, const float* d, float r2, int sidx) {
+            const float mVj = p.hi[j].w;
+            const float rtj = k.rho0 + t.drt[j];
+            const float r = fast_sqrt(r2);
+            float kc[3];
+            grad_c<DIM, CORR>(L, w_grad(k, r), d, kc);
+            const float irj = __fdividef(1.f, rtj * rtj);
+            const float coef = mVj * rtj;
+            // m_ab = sigma_j / rho_j^2 + sigma_i / rho_i^2
+            const float mxx = t.sigt[j] * irj + ai[0];
+            const float myy = t.sigt[n + j] * irj + ai[1];
+            const float mxy = t.sigt[3 * n + j] * irj + ai[3];
+            if (DIM == 3) {
+                const float mzz = t.sigt[2 * n + j] * irj + ai[2];
+                const float mxz = t.sigt[4 * n + j] * irj + ai[4];
+                const float myz = t.sigt[5 * n + j] * irj + ai[5];
+                dv[0].add(coef * (mxx * kc[0] + mxy * kc[1] + mxz * kc[2]));
+                dv[1].add(coef * (mxy * kc[0] + myy * kc[1] + myz * kc[2]));
+                dv[2].add(coef * (mxz * kc[0] + myz * kc[1] + mzz * kc[2]));
+            } else {
+                dv[0].add(coef * (mxx * kc[0] + mxy * kc[1]));
+                dv[1].add(coef * (mxy * kc[0] + myy * kc[1]));
+            }
+            if (DP) vgrad_add<DIM>(mVj, vti, t.vt[j], kc, vg, dd);
+            if (rep_on && tf_type(p.lo[j].w) == MAT_REP) {  // eng/solver_sph_base.py:675-689
+                const float chi = (r > 0.f && r < k.diam) ? 1.f - r / k.diam : 0.f;
+                const float gm = r / k.h075;
+                float fr = 0.f;
+                if (gm > 0.f && gm <= 2.f / 3.f) fr = 2.f / 3.f;
+                else if (gm > 2.f / 3.f && gm <= 1.f) fr = 2.f * gm - 1.5f * gm * gm;
+                else if (gm > 1.f && gm < 2.f) fr = 0.5f * (2.f - gm) * (2.f - gm);
+                const float rs = k.rep_fac * chi * fr / r2;
+                dv[0].add(rs * d[0]);
+                dv[1].add(rs * d[1]);
+                if (DIM == 3) dv[2].add(rs * d[2]);
+            }
+            if ((sidx & 7) == 7) { dv[0].flush(); dv[1].flush(); dv[2].flush(); dd.flush(); }
+        });
+        const float damp = -k.damp_eps * sqrtf(k.damp_E / (rti * k.h2));
+        t.dv[i] = make_float4(dv[0].get() + k.g[0] + damp * vti.x, dv[1].get() + k.g[1] + damp * vti.y,
+                              (DIM == 3 ? dv[2].get() : 0.f) + k.g[2] + damp * vti.z, 0.f);
+        if (DP) {
+            t.dd[i] = dd.get() * rti;
+            float s[6], I1, sJ2, f_old;
+            dp_inv32(k, sti, s, I1, sJ2, f_old);
+            float er[6];
+            strain_rate(vg, er);
+            const float w01 = 0.5f * (vg[1] - vg[3]), w02 = 0.5f * (vg[2] - vg[6]), w12 = 0.5f * (vg[5] - vg[7]);
+            const float W[9] = {0.f, w01, w02, -w01, 0.f, w12, -w02, -w12, 0.f};
+            float S[9];
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) S[3 * a + b] = sti[sym_idx(a, b)];
+            const float tr = (er[0] + er[1]) + er[2];
+            const bool plastic = f_old >= -(float)EPS_F && sJ2 > (float)EPS;
+            const float lam = plastic ? (k.three_aK * tr + (k.Gm / sJ2) * sym_dd(s, er)) / k.lam_den : 0.f;
+            float ds[6];
+            for (int q = 0; q < 6; ++q) {
+                const int a = q < 3 ? q : (q == 5 ? 1 : 0);
+                const int b = q < 3 ? q : (q == 3 ? 1 : 2);
+                // Jaumann term J_ab = sum_k sigma_ak w_bk + sigma_kb w_ak
+                const float J = S[3 * a] * W[3 * b] + S[3 * a + 1] * W[3 * b + 1] + S[3 * a + 2] * W[3 * b + 2] +
+                                S[b] * W[3 * a] + S[3 + b] * W[3 * a + 1] + S[6 + b] * W[3 * a + 2];
+                const float ed = er[q] - (q < 3 ? tr / 3.f : 0.f);
+                const float te = k.twoG * ed + (q < 3 ? k.Km * tr : 0.f);
+                const float tg = plastic ? lam * ((q < 3 ? k.nine_K_sin : 0.f) + k.Gm / sJ2 * s[q]) : 0.f;
+                ds[q] = (J + te) - tg;
+            }
+            store_sym(t.dsig, n, i, ds);
+            t.dee[i] = equiv_rate(er);
+            float dep = 0.f;
+            if (plastic) {
+                // g_p is never written by the reference (eng/particle_func.py:52), so g_p - 0
+                const float gd = sJ2 + 3.f * I1 * k.sin_dila;
+                float ep[6];
+                for (int q = 0; q < 6; ++q) ep[q] = lam * (fabsf(ds[q]) > (float)EPS ? gd / ds[q] : 0.f);
+                dep = equiv_rate(ep);
+            }
+            t.deep[i] = dep;
+        }
+      }
+    });
+}
+
+// mu(I) post-step, part 1 (eng/solver_sph_muI.py:134-149): density clamp, volume, equivalent
+// strain.  stress <- stress_tmp is folded into the regularisation below.
+__global__ void k_post_mui32(K32 k, P32 p, T32 t) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd) return;
+    if (tf_type(p.lo[i].w) != MAT_SOIL) return;
+    const float dr = fmaxf(p.drho[i], 0.f);
+    p.drho[i] = dr;
+    p.hi[i].w = p.mass[i] / (k.rho0 + dr);
+    p.eeq[i] += k.dt * t.dee[i];
+}
+
+// mu(I) stress regularisation (eng/solver_sph_muI.py:151-156): stress_i = CSPM_f_i
+// sum_{soil j} m_Vj stress_tmp_j W_ij at the moved positions, by direct enumeration over
+// the cell table of the last sort (every soil particle; the prefilter positions predate
+// this step's move, so it is off).  Both phases of the reference's racy in-place update
+// are separated: every read is of stress_tmp.
+template <int DIM>
+__global__ void k_reg_mui32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
+                            const int* __restrict__ sstart) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.nd; i += gridDim.x * blockDim.x) {
+        if (tf_type(p.lo[i].w) != MAT_SOIL) continue;
+        const size_t n = k.n;
+        float s[6] = {0, 0, 0, 0, 0, 0};
+        enum_neighbors<DIM>(k, i, p.hi, p.lo, PF, dstart, sstart, false, [&](int j, const float*, float r2) {
+            if (tf_type(p.lo[j].w) != MAT_SOIL) return;
+            const float mw = p.hi[j].w * w_val(k, fast_sqrt(r2));
+            for (int q = 0; q < 6; ++q) s[q] += mw * t.sigt[q * n + j];
+        }, false, false);
+        const float f = t.cf[i];
+        for (int q = 0; q < 6; ++q) p.sig[q * n + i] = s[q] * f;
+    }
+}
+
+// Drucker-Prager post-step (eng/solver_sph_dp.py:277-296).
+__global__ void k_post_dp32(K32 k, P32 p, T32 t) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd) return;
+    if (tf_type(p.lo[i].w) != MAT_SOIL) return;
+    const float dr = fmaxf(p.drho[i], 0.f);
+    p.drho[i] = dr;
+    p.hi[i].w = p.mass[i] / (k.rho0 + dr);
+    float st[6];
+    load_sym(p.sig, k.n, i, st);
+    p.flag[i] = dp_flag32(k, st);
+    dp_adapt32(k, st);
+    store_sym(p.sig, k.n, i, st);
+    p.eeq[i] += k.dt * t.dee[i];
+    p.eeqp[i] += k.dt * t.deep[i];
+}
+
+// Geostatic initial stress (eng/solver_sph_base.py:249-260): sigma_yy = rho0 g_y (y_max - y),
+// sigma_xx = sigma_zz = K0 sigma_yy, from the highest soil particle.
+__global__ void k_ymax32(K32 k, P32 p, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double y = -DBL_MAX;
+    if (i < k.nd && tf_type(p.lo[i].w) == MAT_SOIL) y = k.vs[1] + ((double)p.hi[i].y + (double)p.lo[i].y);
+    for (int o = 16; o > 0; o >>= 1) y = fmax(y, __shfl_down_sync(0xffffffffu, y, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_d(out, y);
+}
+__global__ void k_geostatic32(K32 k, P32 p, const double* ymax, double K0) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd) return;
+    if (tf_type(p.lo[i].w) != MAT_SOIL) return;
+    const double y = k.vs[1] + ((double)p.hi[i].y + (double)p.lo[i].y);
+    const double vs = (double)k.rho0 * (double)k.g[1] * (ymax[0] - y);
+    const size_t n = k.n;
+    p.sig[i] = (float)(K0 * vs);
+    p.sig[n + i] = (float)vs;
+    p.sig[2 * n + i] = (float)(K0 * vs);
+    p.sig[3 * n + i] = p.sig[4 * n + i] = p.sig[5 * n + i] = 0.f;
+}
+
 // ---------------------------------------------------------------- integrators
 __global__ void k_advect_half32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    if (tf_type(p.lo[i].w) <= 0) return;
+    const int ti = tf_type(p.lo[i].w);
+    if (ti <= 0) return;
+    if (ti == MAT_SOIL && k.solver == 3) {
+        const size_t n = k.n;
+        for (int q = 0; q < 6; ++q) t.sigt[q * n + i] += k.hdt * t.dsig[q * n + i];
+    }
     const float drt = t.drt[i] + k.hdt * t.dd[i];
     t.drt[i] = drt;
     p.hi[i].w = p.mass[i] / (k.rho0 + drt);
@@ -709,7 +1115,12 @@ __global__ void k_advect_half32(K32 k, P32 p, T32 t) {
 __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    if (tf_type(p.lo[i].w) <= 0) return;
+    const int ti = tf_type(p.lo[i].w);
+    if (ti <= 0) return;
+    if (ti == MAT_SOIL && k.solver == 3) {
+        const size_t n = k.n;
+        for (int q = 0; q < 6; ++q) p.sig[q * n + i] += k.dt * t.dsig[q * n + i];
+    }
     const float dr = p.drho[i] + k.dt * t.dd[i];
     p.drho[i] = dr;
     p.hi[i].w = p.mass[i] / (k.rho0 + dr);
@@ -831,6 +1242,16 @@ __global__ void k_export(K32 k, P32 p, T32 t, int what, double* out) {
     case 9: { float4 v = t.dv[i]; out[i] = v.x; out[n + i] = v.y; out[2 * n + i] = v.z; break; }
     case 10: out[i] = t.cf[i]; break;
     case 11: for (int q = 0; q < 9; ++q) out[(size_t)q * n + i] = t.L ? t.L[(size_t)q * n + i] : 0.0; break;
+    case 12: case 13: case 14: {  // stress, stress_tmp, d_stress: full 3 x 3 planes from the six stored
+        const float* a = what == 12 ? p.sig : what == 13 ? t.sigt : t.dsig;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) out[(size_t)(3 * r + c) * n + i] = a[(size_t)sym_idx(r, c) * n + i];
+        break;
+    }
+    case 15: out[i] = p.eeq[i]; break;
+    case 16: out[i] = p.eeqp[i]; break;
+    case 17: out[i] = t.dee[i]; break;
+    case 18: out[i] = t.deep[i]; break;
     default: break;
     }
 }
@@ -845,6 +1266,7 @@ __global__ void k_export_int(K32 k, P32 p, int what, int* out) {
     case 2: out[i] = id.y; break;
     case 3: out[i] = id.z; break;
     case 4: out[i] = id.w; break;
+    case 5: out[i] = p.flag ? p.flag[i] : 0; break;
     default: break;
     }
 }
@@ -866,16 +1288,6 @@ __global__ void k_import(K32 k, P32 p, int what, const double* in) {
     case 2: if (tf_type(p.lo[i].w) > 0) p.drho[i] = (float)(in[i] - (double)k.rho0); break;
     case 3: p.vel[i].w = (float)in[i]; break;
     default: break;
-    }
-}
-
-__device__ __forceinline__ void atomic_max_d(double* addr, double v) {
-    unsigned long long* a = reinterpret_cast<unsigned long long*>(addr);
-    unsigned long long old = *a;
-    while (__longlong_as_double(old) < v) {
-        unsigned long long prev = atomicCAS(a, old, __double_as_longlong(v));
-        if (prev == old) break;
-        old = prev;
     }
 }
 
@@ -920,7 +1332,8 @@ __global__ void k_load32(K32 k, const double* __restrict__ x, const double* __re
                          const double* __restrict__ dens, const double* __restrict__ mass,
                          const double* __restrict__ mV, const double* __restrict__ pres,
                          const int* __restrict__ mt, const int* __restrict__ mid, const int* __restrict__ oid,
-                         const int* __restrict__ dyn, const int* __restrict__ slot, P32 p) {
+                         const int* __restrict__ dyn, const int* __restrict__ slot,
+                         const int* __restrict__ scene_of, P32 p) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= k.n) return;
     const int i = slot[s];  // destination index for source particle s
@@ -932,13 +1345,29 @@ __global__ void k_load32(K32 k, const double* __restrict__ x, const double* __re
         lv[d] = (float)(xr - hq);
     }
     // bit 30 keeps the word a normal float, so no denormal flush can touch it in transit
-    const int word = 0x40000000 | (mt[s] & 0xffff) | ((dyn[s] & 1) << 16);
+    const int sc = scene_of ? (scene_of[s] & 0xfff) : 0;
+    const int word = 0x40000000 | (mt[s] & 0xffff) | ((dyn[s] & 1) << 16) | (sc << 17);
     p.hi[i] = make_float4(hv[0], hv[1], hv[2], (float)mV[s]);
     p.lo[i] = make_float4(lv[0], lv[1], lv[2], __int_as_float(word));
     p.vel[i] = make_float4((float)v[3 * (size_t)s], (float)v[3 * (size_t)s + 1], (float)v[3 * (size_t)s + 2], (float)pres[s]);
     p.drho[i] = mt[s] > 0 ? (float)(dens[s] - (double)k.rho0) : 0.f;
     p.mass[i] = (float)mass[s];
     p.ids[i] = make_int4(s, mid[s], oid[s], dyn[s]);
+}
+
+// Upload of the initial stress: (n, 3, 3) row-major -> six planes (upper triangle).
+__global__ void k_load_stress32(K32 k, const double* __restrict__ st, const int* __restrict__ slot, P32 p) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= k.n) return;
+    const int i = slot[s];
+    const size_t n = k.n;
+    const double* a = st + 9 * (size_t)s;
+    p.sig[i] = (float)a[0];
+    p.sig[n + i] = (float)a[4];
+    p.sig[2 * n + i] = (float)a[8];
+    p.sig[3 * n + i] = (float)a[1];
+    p.sig[4 * n + i] = (float)a[2];
+    p.sig[5 * n + i] = (float)a[5];
 }
 
 __global__ void k_deinterleave32(const double* src, double* dst, int n, int k) {
@@ -960,7 +1389,8 @@ __global__ void k_nbr_count32(K32 k, const float4* HI, const float4* LO, const f
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     int m = 0;
-    enum_neighbors<DIM>(k, i, HI, LO, PF, ds, ss, is_flow(tf_type(PF[i].w)), [&](int, const float*, float) { ++m; });
+    enum_neighbors<DIM>(k, i, HI, LO, PF, ds, ss, is_flow(tf_type(PF[i].w)), [&](int, const float*, float) { ++m; },
+                        false, false);
     counts[i] = m;
 }
 
@@ -971,7 +1401,7 @@ __global__ void k_nbr_fill32(K32 k, const float4* HI, const float4* LO, const fl
     if (i >= k.n) return;
     int m = off[i];
     enum_neighbors<DIM>(k, i, HI, LO, PF, ds, ss, is_flow(tf_type(PF[i].w)),
-                        [&](int j, const float*, float) { list[m++] = j; });
+                        [&](int j, const float*, float) { list[m++] = j; }, false, false);
 }
 
 template <int DIM>
@@ -1027,6 +1457,81 @@ __global__ void k_disp32(K32 k, const float4* __restrict__ HI, const float4* __r
     if ((threadIdx.x & 31) == 0 && d2 > 0.f) atomicMax(maxd, __float_as_uint(d2));
 }
 
+// List occupancy: out[0] / out[1] += stored entries (min(count, capacity)) of the dynamic /
+// static block, out[2] += overflowed particles (each thread classifies its own particle).
+__global__ void k_list_stats(K32 k, const int* __restrict__ cnt, unsigned long long* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long ed = 0, es = 0, o = 0;
+    if (i < k.n) {
+        const int m = cnt[i];
+        const unsigned long long e = (unsigned long long)(m < k.maxn ? m : k.maxn);
+        if (i < k.nd) ed = e; else es = e;
+        o = m > k.maxn ? 1ull : 0ull;
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        ed += __shfl_down_sync(0xffffffffu, ed, d);
+        es += __shfl_down_sync(0xffffffffu, es, d);
+        o += __shfl_down_sync(0xffffffffu, o, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (ed) atomicAdd(&out[0], ed);
+        if (es) atomicAdd(&out[1], es);
+        if (o) atomicAdd(&out[2], o);
+    }
+}
+
+// Per-scene FP64 diagnostics of a batched ensemble (out[8 * scene + q], q as k_diag32;
+// positions relative to the scene's own origin, x - scene * pitch).  Warps whose flow
+// particles all belong to one scene reduce before their atomics.
+__global__ void k_diag_batch32(K32 k, P32 p, double pitch, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, -DBL_MAX};
+    int sc = -1;
+    if (i < k.nd) {
+        const float w = p.lo[i].w;
+        if (is_flow(tf_type(w))) {
+            sc = tf_scene(w);
+            const double m = p.mass[i];
+            const float4 vv = p.vel[i];
+            const float4 h = p.hi[i], l = p.lo[i];
+            const double x = k.vs[0] + ((double)h.x + (double)l.x) - sc * pitch;
+            const double y = k.vs[1] + ((double)h.y + (double)l.y);
+            const double z = k.vs[2] + ((double)h.z + (double)l.z);
+            const double v2 = (double)vv.x * vv.x + (double)vv.y * vv.y + (double)vv.z * vv.z;
+            v[0] = m; v[1] = m * vv.x; v[2] = m * vv.y; v[3] = m * vv.z; v[4] = 0.5 * m * v2;
+            v[5] = -m * ((double)k.g[0] * x + (double)k.g[1] * y + (double)k.g[2] * z);
+            v[6] = sqrt(v2); v[7] = x;
+        }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, sc);
+    if (peers == 0xffffffffu) {
+        if (sc < 0) return;
+        for (int o = 16; o > 0; o >>= 1) {
+            for (int q = 0; q < 6; ++q) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+            v[6] = fmax(v[6], __shfl_down_sync(0xffffffffu, v[6], o));
+            v[7] = fmax(v[7], __shfl_down_sync(0xffffffffu, v[7], o));
+        }
+        if ((threadIdx.x & 31) != 0) return;
+    } else if (sc < 0) {
+        return;
+    }
+    double* o8 = out + 8 * (size_t)sc;
+    for (int q = 0; q < 6; ++q) atomicAdd(&o8[q], v[q]);
+    atomic_max_d(&o8[6], v[6]);
+    atomic_max_d(&o8[7], v[7]);
+}
+
+// Graph mode: decide on the device whether this step re-sorts and rebuilds the lists
+// (largest displacement since the last build above 0.45 skin), by setting the condition
+// of the graph's IF node; count the rebuilds.
+__global__ void k_set_rebuild32(cudaGraphConditionalHandle hnd, const unsigned* __restrict__ maxd, float limit,
+                                int* __restrict__ counter) {
+    const float d2 = __uint_as_float(*maxd);
+    const unsigned r = !(d2 <= limit) ? 1u : 0u;
+    cudaGraphSetConditional(hnd, r);
+    if (r) atomicAdd(counter, 1);
+}
+
 }  // namespace
 
 // ====================================================================== host side
@@ -1049,6 +1554,23 @@ struct Fp32State {
     std::vector<void*> allocs;
     std::vector<std::pair<std::string, double*>> views;
     bool lists_valid = false;
+    long long rebuilds = 0;        // list builds since creation
+    int nscenes = 0;               // > 0 for a batched ensemble
+    // launch configuration (tsg_set_launch / tsg_autotune): threads per block of the
+    // neighbour kernels, cells per CTA of the warp-per-cell list build (0: one thread per
+    // particle), steps per captured graph
+    int tpb = 128, cells_per_cta = 4, steps_per_graph = 1;
+    // captured step graphs: [0] one step, [1] steps_per_graph steps
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        int steps = 0, cur = -1, tpb = 0, cpc = 0;
+        bool collide = false;
+        long long kernels = 0;    // kernel nodes outside the conditional rebuild bodies
+    } graphs[2];
+    long long body_kernels = 0;   // kernel nodes of one rebuild body
+    int* d_rebuilds = nullptr;    // rebuilds taken by graph replays (device counter)
+    int rebuilds_seen = 0;        // part of d_rebuilds already folded into the counters
+    void* snap = nullptr;         // autotuner snapshot of the particle state
 };
 
 namespace {
@@ -1110,9 +1632,9 @@ __global__ void k_offset(int* a, long long m, int off) {
 }  // namespace
 
 int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp, bool from_device,
-                Fp32State** out, cudaStream_t s) {
+                Fp32State** out, cudaStream_t s, const Fp32Scenes* scenes) {
     *out = nullptr;
-    if (c.solver != 1 || c.ti == 4) return TSG_E_UNSUPPORTED;  // WCSPH with SE / LF in this form
+    if (c.ti == 4) return TSG_E_UNSUPPORTED;  // SE / LF in this form
     Fp32State* st = new Fp32State();
     st->c = c;
     const int n = c.n;
@@ -1139,6 +1661,11 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     k.visc_fac = (float)c.visc_fac; k.eps_h2 = (float)c.eps_h2; k.rho0 = (float)c.rho0; k.B = (float)c.B;
     k.gamma = (float)c.gamma; k.dt = (float)c.dt; k.hdt = (float)c.hdt;
     k.rep_fac = (float)c.rep_fac; k.diam = (float)c.diam; k.h075 = (float)c.h075; k.r_eps = (float)c.r_eps;
+    k.mu = (float)c.mu; k.c2 = (float)c.vsound2; k.coh = (float)c.coh; k.alpha = (float)c.alpha;
+    k.k_c = (float)c.k_c; k.kc_over_alpha = (float)c.kc_over_alpha; k.Gm = (float)c.Gm; k.Km = (float)c.Km;
+    k.sin_dila = (float)c.sin_dila; k.lam_den = (float)c.lam_den; k.three_aK = (float)c.three_aK;
+    k.nine_K_sin = (float)c.nine_K_sin; k.twoG = (float)c.twoG;
+    k.damp_eps = (float)c.damp_eps; k.damp_E = (float)c.damp_E; k.h2 = (float)c.h2;
     // Verlet skin: lists hold pairs within R + skin and stay valid while no particle has moved
     // more than skin / 2 since they were built (0.45 skin for margin on f32 positions)
     const double skin = cfg.list_skin > 0 ? cfg.list_skin * c.R : 0.0;
@@ -1172,9 +1699,14 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     st->nd = nd;
     k.nd = nd;
     // allocations
+    const bool soil = c.solver != 1;
     for (int q = 0; q < 2; ++q) {
         st->P[q].hi = dal<float4>(*st, n); st->P[q].lo = dal<float4>(*st, n); st->P[q].vel = dal<float4>(*st, n);
         st->P[q].drho = dal<float>(*st, n); st->P[q].mass = dal<float>(*st, n); st->P[q].ids = dal<int4>(*st, n);
+        if (soil) {
+            st->P[q].sig = dal<float>(*st, 6 * (size_t)n); st->P[q].eeq = dal<float>(*st, n);
+            st->P[q].eeqp = dal<float>(*st, n); st->P[q].flag = dal<int>(*st, n);
+        }
     }
     T32& t = st->T;
     t.vt = dal<float4>(*st, n); t.pr = dal<float2>(*st, n); t.drt = dal<float>(*st, n); t.dd = dal<float>(*st, n);
@@ -1182,6 +1714,10 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     t.L = c.corr == 1 ? dal<float>(*st, 9 * (size_t)n) : nullptr;
     t.cnt = dal<int>(*st, n);
     t.nbr = dal<int>(*st, (size_t)k.maxn * n);
+    if (soil) {
+        t.sigt = dal<float>(*st, 6 * (size_t)n); t.dee = dal<float>(*st, n);
+        if (c.solver == 3) { t.dsig = dal<float>(*st, 6 * (size_t)n); t.deep = dal<float>(*st, n); }
+    }
     st->pf = dal<float4>(*st, n);
     const size_t nb = (size_t)k.G + 1;
     st->dcount = dal<int>(*st, nb); st->dstart = dal<int>(*st, nb + 1);
@@ -1191,6 +1727,8 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     st->cells_d = dal<int>(*st, nb); st->cells_s = dal<int>(*st, nb); st->ncells = dal<int>(*st, 2);
     st->ovf_list = dal<int>(*st, n); st->novf = dal<int>(*st, 1);
     st->maxdisp = dal<unsigned>(*st, 1);
+    st->d_rebuilds = dal<int>(*st, 1);
+    st->cells_per_cta = c.dim == 3 ? 4 : 0;
     st->stage = dal<double>(*st, 9 * (size_t)n + 16);
     st->scratch = dal<double>(*st, 64);
     if (!t.nbr || !st->stage) { fp32_destroy(st); return TSG_E_CUDA; }
@@ -1219,7 +1757,29 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     cudaMemcpyAsync(ioid, pp->obj_id, sizeof(int) * n, kind, s);
     cudaMemcpyAsync(idyn, pp->is_dynamic, sizeof(int) * n, kind, s);
     cudaMemcpyAsync(islot, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
-    TSG_LAUNCH(k_load32, nblk(n), TPB, s, k, dx, dv, d1, d2, d3, d4, imt, imid, ioid, idyn, islot, st->P[0]);
+    int* iscene = nullptr;
+    if (scenes && scenes->nscenes > 0) {
+        if (scenes->nscenes > kMaxScenes) { fp32_destroy(st); return TSG_E_CAPACITY; }
+        iscene = st->cell_of;  // scratch until the first sort
+        cudaMemcpyAsync(iscene, scenes->scene_of, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+        std::vector<float2> par(scenes->nscenes);
+        for (int q = 0; q < scenes->nscenes; ++q) par[q] = make_float2(scenes->stiffness[q], scenes->visc_fac[q]);
+        float2* dpar = dal<float2>(*st, scenes->nscenes);
+        if (!dpar) { fp32_destroy(st); return TSG_E_CUDA; }
+        cudaMemcpyAsync(dpar, par.data(), sizeof(float2) * scenes->nscenes, cudaMemcpyHostToDevice, s);
+        cudaStreamSynchronize(s);
+        k.scene_par = dpar;
+        st->nscenes = scenes->nscenes;
+    }
+    TSG_LAUNCH(k_load32, nblk(n), TPB, s, k, dx, dv, d1, d2, d3, d4, imt, imid, ioid, idyn, islot, iscene, st->P[0]);
+    if (soil && pp->stress) {  // (n, 3, 3) row-major -> six planes (upper triangle)
+        double* sst = nullptr;
+        if (cudaMalloc(&sst, sizeof(double) * 9 * (size_t)n) != cudaSuccess) { fp32_destroy(st); return TSG_E_CUDA; }
+        cudaMemcpyAsync(sst, pp->stress, sizeof(double) * 9 * n, kind, s);
+        TSG_LAUNCH(k_load_stress32, nblk(n), TPB, s, k, sst, islot, st->P[0]);
+        cudaStreamSynchronize(s);
+        cudaFree(sst);
+    }
     cudaStreamSynchronize(s);
     cudaMemsetAsync(st->P[1].hi, 0, sizeof(float4) * n, s);
     cudaMemsetAsync(st->P[1].lo, 0, sizeof(float4) * n, s);
@@ -1239,11 +1799,26 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
         cudaMemcpyAsync(dst.drho + off, src.drho + off, sizeof(float) * ns, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(dst.mass + off, src.mass + off, sizeof(float) * ns, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(dst.ids + off, src.ids + off, sizeof(int4) * ns, cudaMemcpyDeviceToDevice, s);
+        if (soil) {
+            for (int q = 0; q < 6; ++q)
+                cudaMemcpyAsync(dst.sig + q * (size_t)n + off, src.sig + q * (size_t)n + off, sizeof(float) * ns,
+                                cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(dst.eeq + off, src.eeq + off, sizeof(float) * ns, cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(dst.eeqp + off, src.eeqp + off, sizeof(float) * ns, cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(dst.flag + off, src.flag + off, sizeof(int) * ns, cudaMemcpyDeviceToDevice, s);
+        }
     } else {
         cudaMemsetAsync(st->sstart, 0, sizeof(int) * (k.G + 2), s);
     }
     cudaMemsetAsync(st->ncells + 1, 0, sizeof(int), s);
     TSG_LAUNCH(k_nonempty_cells, nblk(k.G, 256), 256, s, (long long)k.G, st->sstart, st->cells_s, st->ncells + 1);
+    if (c.solver == 3 && cfg.init_geostatic && nd > 0) {  // eng/solver_sph_dp.py:35 -> init_stress
+        double lo = -DBL_MAX;
+        cudaMemcpyAsync(st->scratch, &lo, sizeof lo, cudaMemcpyHostToDevice, s);
+        TSG_LAUNCH(k_ymax32, nblk(nd), TPB, s, k, st->P[0], st->scratch);
+        TSG_LAUNCH(k_geostatic32, nblk(nd), TPB, s, k, st->P[0], st->scratch, c.K0);
+        cudaStreamSynchronize(s);
+    }
     // the dynamic block of both buffers must agree before the first sort
     cudaStreamSynchronize(s);
     if (cudaGetLastError() != cudaSuccess) { fp32_destroy(st); return TSG_E_CUDA; }
@@ -1253,48 +1828,113 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
 
 void fp32_destroy(Fp32State* st) {
     if (!st) return;
+    for (auto& g : st->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (st->snap) cudaFree(st->snap);
     for (void* p : st->allocs) cudaFree(p);
     delete st;
 }
 
-void fp32_sort(Fp32State& st, cudaStream_t s) {
+namespace {
+
+template <int DIM, int WPB>
+void lists_by_cell(Fp32State& st, const P32& p, cudaStream_t s) {
+    const K32& k = st.k;
+    const int nb = 152 * 64 / WPB;
+    TSG_LAUNCH((k_lists_cell<DIM, WPB>), nb, 32 * WPB, s, k, 0, st.cells_d, st.ncells, p.hi, p.lo, st.pf, st.dstart,
+               st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
+    TSG_LAUNCH((k_lists_cell<DIM, WPB>), nb, 32 * WPB, s, k, 1, st.cells_s, st.ncells + 1, p.hi, p.lo, st.pf,
+               st.dstart, st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
+}
+
+template <int DIM>
+void build_lists(Fp32State& st, const P32& p, cudaStream_t s) {
+    const K32& k = st.k;
+    cudaMemsetAsync(st.novf, 0, sizeof(int), s);
+    if (st.cells_per_cta <= 0) {  // one thread per particle
+        TSG_LAUNCH(k_lists<DIM>, nblk(k.n), TPB, s, k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr,
+                   st.ovf_list, st.novf);
+        return;
+    }
+    cudaMemsetAsync(st.ncells, 0, sizeof(int), s);
+    TSG_LAUNCH(k_nonempty_cells, nblk(k.G, 256), 256, s, (long long)k.G, st.dstart, st.cells_d, st.ncells);
+    switch (st.cells_per_cta) {
+    case 2: lists_by_cell<DIM, 2>(st, p, s); break;
+    case 8: lists_by_cell<DIM, 8>(st, p, s); break;
+    default: lists_by_cell<DIM, 4>(st, p, s); break;
+    }
+    // particles in the out-of-grid bins (bounds read on the device), then particles whose
+    // true cell differs from their storage cell
+    TSG_LAUNCH(k_lists_range<DIM>, 64, TPB, s, k, st.dstart + k.G, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt,
+               st.T.nbr, st.ovf_list, st.novf);
+    TSG_LAUNCH(k_lists_range<DIM>, 64, TPB, s, k, st.sstart + k.G, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt,
+               st.T.nbr, st.ovf_list, st.novf);
+    TSG_LAUNCH(k_lists_fixup<DIM>, 2 * 152, TPB, s, k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr,
+               st.ovf_list, st.novf);
+}
+
+// Copy the dynamic block of b back into a (graph mode keeps one current buffer).
+__global__ void k_copy_back32(int nd, P32 b, P32 a, size_t n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nd) return;
+    a.hi[i] = b.hi[i];
+    a.lo[i] = b.lo[i];
+    a.vel[i] = b.vel[i];
+    a.drho[i] = b.drho[i];
+    a.mass[i] = b.mass[i];
+    a.ids[i] = b.ids[i];
+    if (a.sig) {
+        for (int q = 0; q < 6; ++q) a.sig[q * n + i] = b.sig[q * n + i];
+        a.eeq[i] = b.eeq[i];
+        a.eeqp[i] = b.eeqp[i];
+        a.flag[i] = b.flag[i];
+    }
+}
+
+// Re-sort the dynamic block and rebuild every list.  in_place keeps the current buffer
+// (the sorted block is copied back), as a captured graph needs fixed pointers.
+void rebuild(Fp32State& st, cudaStream_t s, bool in_place) {
     {
         PhaseScope ph(s, PH_SORT);
         if (st.nd > 0) {
             build_cells(st, 0, st.nd, st.dcount, st.dstart, s, true);
-            st.cur = 1 - st.cur;
+            if (in_place) TSG_LAUNCH(k_copy_back32, nblk(st.nd), TPB, s, st.nd, st.P[1 - st.cur], st.P[st.cur], (size_t)st.n);
+            else st.cur = 1 - st.cur;
         } else {
             cudaMemsetAsync(st.dstart, 0, sizeof(int) * (st.k.G + 2), s);
         }
     }
-    const K32& k = st.k;
-    P32& p = st.P[st.cur];
     {
         PhaseScope ph2(s, PH_LISTS);
-        cudaMemsetAsync(st.novf, 0, sizeof(int), s);
-        if (k.dim == 3) {
-            cudaMemsetAsync(st.ncells, 0, sizeof(int), s);
-            TSG_LAUNCH(k_nonempty_cells, nblk(k.G, 256), 256, s, (long long)k.G, st.dstart, st.cells_d, st.ncells);
-            const int nb = 152 * 16;
-            TSG_LAUNCH(k_lists_cell<3>, nb, 128, s, k, 0, st.cells_d, st.ncells, p.hi, p.lo, st.pf, st.dstart,
-                       st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
-            TSG_LAUNCH(k_lists_cell<3>, nb, 128, s, k, 1, st.cells_s, st.ncells + 1, p.hi, p.lo, st.pf, st.dstart,
-                       st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
-            // particles in the out-of-grid bins (bounds read on the device)
-            TSG_LAUNCH(k_lists_range<3>, 64, TPB, s, k, st.dstart + k.G, p.hi, p.lo, st.pf, st.dstart,
-                       st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
-            TSG_LAUNCH(k_lists_range<3>, 64, TPB, s, k, st.sstart + k.G, p.hi, p.lo, st.pf, st.dstart,
-                       st.sstart, st.T.cnt, st.T.nbr, st.ovf_list, st.novf);
-            TSG_LAUNCH(k_lists_fixup<3>, 2 * 152, TPB, s, k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt,
-                       st.T.nbr, st.ovf_list, st.novf);
-        } else {
-            TSG_LAUNCH(k_lists<2>, nblk(k.n), TPB, s, k, p.hi, p.lo, st.pf, st.dstart, st.sstart, st.T.cnt, st.T.nbr,
-                       st.ovf_list, st.novf);
-        }
+        if (st.k.dim == 3) build_lists<3>(st, st.P[st.cur], s);
+        else build_lists<2>(st, st.P[st.cur], s);
     }
     cudaMemsetAsync(st.maxdisp, 0, sizeof(unsigned), s);
+}
+
+}  // namespace
+
+void fp32_sort(Fp32State& st, cudaStream_t s) {
+    rebuild(st, s, false);
     st.lists_valid = true;
     st.built = true;
+    ++st.rebuilds;
+}
+
+int fp32_list_stats(Fp32State& st, int64_t* out4, cudaStream_t s) {
+    if (!st.built) return TSG_E_STATE;
+    fp32_flush_counters(st, s);
+    unsigned long long* acc = reinterpret_cast<unsigned long long*>(st.scratch);
+    cudaMemsetAsync(acc, 0, 3 * sizeof(unsigned long long), s);
+    TSG_LAUNCH(k_list_stats, nblk(st.k.n), TPB, s, st.k, st.T.cnt, acc);
+    unsigned long long h[3] = {0, 0, 0};
+    cudaMemcpyAsync(h, acc, sizeof h, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    out4[0] = (int64_t)h[0];
+    out4[1] = (int64_t)h[1];
+    out4[2] = (int64_t)h[2];
+    out4[3] = st.rebuilds;
+    return 0;
 }
 
 bool fp32_rebuild_due(Fp32State& st, cudaStream_t s) {
@@ -1315,10 +1955,10 @@ void fp32_kernel_corr(Fp32State& st, cudaStream_t s) {
     const K32& k = st.k;
     const Ovf ovf{st.ovf_list, st.novf};
     if (k.dim == 2) {
-        TSG_LAUNCH((k_corr32<2, false>), nblk(k.n), TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
+        TSG_LAUNCH((k_corr32<2, false>), nblk(k.n, st.tpb), st.tpb, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
         TSG_LAUNCH((k_corr32<2, true>), 64, TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
     } else {
-        TSG_LAUNCH((k_corr32<3, false>), nblk(k.n), TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
+        TSG_LAUNCH((k_corr32<3, false>), nblk(k.n, st.tpb), st.tpb, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
         TSG_LAUNCH((k_corr32<3, true>), 64, TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
     }
 }
@@ -1328,9 +1968,55 @@ void fp32_init_tmp(Fp32State& st, cudaStream_t s) {
     TSG_LAUNCH(k_init_tmp32, nblk(st.k.n), TPB, s, st.k, st.P[st.cur], st.T);
 }
 
+// mu(I) / Drucker-Prager one_step (eng/solver_sph_muI.py:62-131, eng/solver_sph_dp.py:210-274).
+template <int DIM>
+void soil_one_step(Fp32State& st, cudaStream_t s) {
+    const K32& k = st.k;
+    P32& p = st.P[st.cur];
+    const Ovf ovf{st.ovf_list, st.novf};
+    const int nb = nblk(k.nd, st.tpb);
+    {
+        PhaseScope ph(s, PH_PRE);
+        if (k.solver == 2) {
+            if (k.corr) { TSG_LAUNCH((k_mui_stress32<DIM, false, true>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                          TSG_LAUNCH((k_mui_stress32<DIM, true, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
+            else { TSG_LAUNCH((k_mui_stress32<DIM, false, false>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                   TSG_LAUNCH((k_mui_stress32<DIM, true, false>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
+        } else {
+            TSG_LAUNCH(k_pre_dp32, nblk(k.nd), TPB, s, k, p, st.T);
+        }
+    }
+    {
+        PhaseScope ph(s, PH_BDY);
+        auto bdy = [&](int base, int count_n) {
+            if (count_n <= 0) return;
+            TSG_LAUNCH((k_bdy_soil32<DIM, false>), nblk(count_n, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+            TSG_LAUNCH((k_bdy_soil32<DIM, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+        };
+        bdy(k.nd, k.n - k.nd);
+        if (st.c.n_bdy > k.n - k.nd) bdy(0, k.nd);
+    }
+    {
+        PhaseScope ph(s, PH_RATES);
+#define SOIL_MOM(CORR, DP)                                                                                       \
+        do {                                                                                                     \
+            TSG_LAUNCH((k_soil_mom32<DIM, false, CORR, DP>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); \
+            TSG_LAUNCH((k_soil_mom32<DIM, true, CORR, DP>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);  \
+        } while (0)
+        if (k.solver == 2) { if (k.corr) SOIL_MOM(true, false); else SOIL_MOM(false, false); }
+        else { if (k.corr) SOIL_MOM(true, true); else SOIL_MOM(false, true); }
+#undef SOIL_MOM
+    }
+}
+
 void fp32_one_step(Fp32State& st, cudaStream_t s) {
     const K32& k = st.k;
     P32& p = st.P[st.cur];
+    if (k.solver != 1) {
+        if (k.dim == 2) soil_one_step<2>(st, s);
+        else soil_one_step<3>(st, s);
+        return;
+    }
     {
         PhaseScope ph(s, PH_PRE);
         TSG_LAUNCH(k_pre32, nblk(k.nd), TPB, s, k, p, st.T);
@@ -1341,10 +2027,10 @@ void fp32_one_step(Fp32State& st, cudaStream_t s) {
         auto bdy = [&](int base, int count_n) {
             if (count_n <= 0) return;
             if (k.dim == 2) {
-                TSG_LAUNCH((k_bdy32<2, false>), nblk(count_n), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+                TSG_LAUNCH((k_bdy32<2, false>), nblk(count_n, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
                 TSG_LAUNCH((k_bdy32<2, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
             } else {
-                TSG_LAUNCH((k_bdy32<3, false>), nblk(count_n), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+                TSG_LAUNCH((k_bdy32<3, false>), nblk(count_n, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
                 TSG_LAUNCH((k_bdy32<3, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
             }
         };
@@ -1354,16 +2040,16 @@ void fp32_one_step(Fp32State& st, cudaStream_t s) {
     {
         PhaseScope ph(s, PH_RATES);
         const Ovf ovf{st.ovf_list, st.novf};
-        const int nb = nblk(k.nd);
+        const int nb = nblk(k.nd, st.tpb);
         if (k.dim == 2) {
-            if (k.corr) { TSG_LAUNCH((k_rates32<2, false, true>), nb, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+            if (k.corr) { TSG_LAUNCH((k_rates32<2, false, true>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
                           TSG_LAUNCH((k_rates32<2, true, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
-            else { TSG_LAUNCH((k_rates32<2, false, false>), nb, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+            else { TSG_LAUNCH((k_rates32<2, false, false>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
                    TSG_LAUNCH((k_rates32<2, true, false>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
         } else {
-            if (k.corr) { TSG_LAUNCH((k_rates32<3, false, true>), nb, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+            if (k.corr) { TSG_LAUNCH((k_rates32<3, false, true>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
                           TSG_LAUNCH((k_rates32<3, true, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
-            else { TSG_LAUNCH((k_rates32<3, false, false>), nb, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+            else { TSG_LAUNCH((k_rates32<3, false, false>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
                    TSG_LAUNCH((k_rates32<3, true, false>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
         }
     }
@@ -1380,10 +2066,10 @@ void fp32_advect(Fp32State& st, int which, cudaStream_t s) {
         if (k.xsph) {
             const Ovf ovf{st.ovf_list, st.novf};
             if (k.dim == 2) {
-                TSG_LAUNCH((k_xsph32<2, false>), nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                TSG_LAUNCH((k_xsph32<2, false>), nblk(k.nd, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
                 TSG_LAUNCH((k_xsph32<2, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
             } else {
-                TSG_LAUNCH((k_xsph32<3, false>), nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+                TSG_LAUNCH((k_xsph32<3, false>), nblk(k.nd, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
                 TSG_LAUNCH((k_xsph32<3, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
             }
         }
@@ -1391,13 +2077,313 @@ void fp32_advect(Fp32State& st, int which, cudaStream_t s) {
         if (k.disp2_limit <= 0.f) st.lists_valid = false;
         break;
     }
-    case TSG_ADVECT_SOMETHING: { PhaseScope ph(s, PH_POST); TSG_LAUNCH(k_post_wc32, nblk(k.nd), TPB, s, k, p); break; }
+    case TSG_ADVECT_SOMETHING: {
+        PhaseScope ph(s, PH_POST);
+        if (k.solver == 1) TSG_LAUNCH(k_post_wc32, nblk(k.nd), TPB, s, k, p);
+        else if (k.solver == 2) {
+            TSG_LAUNCH(k_post_mui32, nblk(k.nd), TPB, s, k, p, st.T);
+            if (k.dim == 2) TSG_LAUNCH(k_reg_mui32<2>, nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart);
+            else TSG_LAUNCH(k_reg_mui32<3>, nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart);
+        } else TSG_LAUNCH(k_post_dp32, nblk(k.nd), TPB, s, k, p, st.T);
+        break;
+    }
     case TSG_ENFORCE_BOUNDARY: { PhaseScope ph(s, PH_OTHER); TSG_LAUNCH(k_enforce32, nblk(k.nd), TPB, s, k, p); break; }
     default: break;
     }
 }
 
 void fp32_rk_update(Fp32State&, int, cudaStream_t) {}
+
+// ---------------------------------------------------------------- captured steps
+namespace {
+
+// One SPHBase.step() after the (conditional) re-sort: kernel correction, init_real2tmp,
+// the integrator's one_step / advect sequence, advect_pos, advect_something and, in
+// collision mode, enforce_boundary (eng/solver_sph_base.py:41-61, :79-120).
+void step_body(Fp32State& st, cudaStream_t s, bool collide) {
+    fp32_kernel_corr(st, s);
+    fp32_init_tmp(st, s);
+    fp32_one_step(st, s);
+    if (st.c.ti == 2) {
+        fp32_advect(st, TSG_ADVECT_LF_HALF, s);
+        fp32_one_step(st, s);
+    }
+    fp32_advect(st, TSG_ADVECT_FULL, s);
+    fp32_advect(st, TSG_ADVECT_POS, s);
+    fp32_advect(st, TSG_ADVECT_SOMETHING, s);
+    if (collide) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
+}
+
+// Fold the device rebuild counter into the host counters (synchronises s).
+void fold_rebuilds(Fp32State& st, cudaStream_t s) {
+    int n = 0;
+    cudaMemcpyAsync(&n, st.d_rebuilds, sizeof n, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    const int delta = n - st.rebuilds_seen;
+    if (delta > 0) {
+        st.rebuilds += delta;
+        add_launches((long long)delta * st.body_kernels);
+        st.rebuilds_seen = n;
+    }
+}
+
+// Capture `steps` steps into one executable graph.  Each step: displacement check, then an
+// IF node whose body re-sorts in place and rebuilds the lists, then the step body.
+int capture_steps(Fp32State& st, int steps, bool collide, Fp32State::StepGraph& g) {
+    cudaStream_t cs = nullptr, bs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return TSG_E_CUDA;
+    if (cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) != cudaSuccess) { cudaStreamDestroy(cs); return TSG_E_CUDA; }
+    const K32& k = st.k;
+    const long long c0 = launch_total();
+    long long body = 0;
+    int rc = 0;
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) rc = TSG_E_CUDA;
+    for (int q = 0; q < steps && !rc; ++q) {
+        cudaStreamCaptureStatus status;
+        cudaGraph_t cg = nullptr;
+        if (cudaStreamGetCaptureInfo(cs, &status, nullptr, &cg) != cudaSuccess || !cg) { rc = TSG_E_CUDA; break; }
+        cudaGraphConditionalHandle hnd;
+        if (cudaGraphConditionalHandleCreate(&hnd, cg, 0, cudaGraphCondAssignDefault) != cudaSuccess) { rc = TSG_E_CUDA; break; }
+        P32& p = st.P[st.cur];
+        TSG_LAUNCH(k_disp32, nblk(k.nd), TPB, cs, k, p.hi, p.lo, st.pf, st.maxdisp);
+        TSG_LAUNCH(k_set_rebuild32, 1, 1, cs, hnd, st.maxdisp, k.disp2_limit, st.d_rebuilds);
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        if (cudaStreamGetCaptureInfo(cs, &status, nullptr, &cg, &deps, nullptr, &ndeps) != cudaSuccess) { rc = TSG_E_CUDA; break; }
+        // (the union inside has no default constructor: zeroed storage, then fields)
+        alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+        std::memset(cp_buf, 0, sizeof cp_buf);
+        cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = hnd;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (cudaGraphAddNode(&node, cg, deps, nullptr, ndeps, &cp) != cudaSuccess) { rc = TSG_E_CUDA; break; }
+        cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+        if (cudaStreamUpdateCaptureDependencies(cs, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess) {
+            rc = TSG_E_CUDA;
+            break;
+        }
+        const long long b0 = launch_total();
+        if (cudaStreamBeginCaptureToGraph(bs, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+            rc = TSG_E_CUDA;
+            break;
+        }
+        rebuild(st, bs, true);
+        cudaGraph_t done = nullptr;
+        if (cudaStreamEndCapture(bs, &done) != cudaSuccess) { rc = TSG_E_CUDA; break; }
+        body = launch_total() - b0;
+        step_body(st, cs, collide);
+    }
+    cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    if (!rc && (e != cudaSuccess || !graph)) rc = TSG_E_CUDA;
+    const long long captured = launch_total() - c0;
+    add_launches(-captured);  // nodes, not launches
+    if (!rc) {
+        if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+        if (cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess) { rc = TSG_E_CUDA; g.exec = nullptr; }
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(bs);
+    cudaStreamDestroy(cs);
+    cudaGetLastError();
+    if (rc) return rc;
+    g.steps = steps;
+    g.cur = st.cur;
+    g.tpb = st.tpb;
+    g.cpc = st.cells_per_cta;
+    g.collide = collide;
+    g.kernels = captured - body * steps;
+    st.body_kernels = body;
+    return 0;
+}
+
+Fp32State::StepGraph* graph_for(Fp32State& st, int steps, bool collide, int* rc) {
+    Fp32State::StepGraph& g = st.graphs[steps == 1 ? 0 : 1];
+    *rc = 0;
+    if (g.exec && g.steps == steps && g.cur == st.cur && g.tpb == st.tpb && g.cpc == st.cells_per_cta &&
+        g.collide == collide)
+        return &g;
+    *rc = capture_steps(st, steps, collide, g);
+    return *rc ? nullptr : &g;
+}
+
+}  // namespace
+
+int fp32_step_graph(Fp32State& st, int nsteps, bool collide, cudaStream_t s) {
+    if (profiling_on()) return TSG_E_STATE;  // per-phase events need the eager path
+    if (!st.built) fp32_sort(st, s);
+    const int K = st.steps_per_graph > 1 ? st.steps_per_graph : 1;
+    int rc = 0;
+    while (nsteps > 0) {
+        const int take = (K > 1 && nsteps >= K) ? K : 1;
+        Fp32State::StepGraph* g = graph_for(st, take, collide, &rc);
+        if (!g) return rc;
+        if (cudaGraphLaunch(g->exec, s) != cudaSuccess) return TSG_E_CUDA;
+        add_launches(g->kernels);
+        nsteps -= take;
+    }
+    st.lists_valid = st.k.disp2_limit > 0.f;
+    return 0;
+}
+
+void fp32_flush_counters(Fp32State& st, cudaStream_t s) { fold_rebuilds(st, s); }
+
+void fp32_get_launch(const Fp32State& st, int* tpb, int* cpc, int* spg) {
+    *tpb = st.tpb;
+    *cpc = st.cells_per_cta;
+    *spg = st.steps_per_graph;
+}
+
+int fp32_set_launch(Fp32State& st, int tpb, int cpc, int spg) {
+    if (tpb != 64 && tpb != 128 && tpb != 256 && tpb != 512) return TSG_E_ARG;
+    if (cpc != 0 && cpc != 2 && cpc != 4 && cpc != 8) return TSG_E_ARG;
+    if (spg < 1 || spg > 64) return TSG_E_ARG;
+    st.tpb = tpb;
+    st.cells_per_cta = cpc;
+    st.steps_per_graph = spg;
+    return 0;
+}
+
+// ---------------------------------------------------------------- autotuner
+namespace {
+
+// Particle state that carries from one step to the next: the current buffer of every
+// persistent array and the boundary particles' v_tmp (the mu(I) first loop reads the
+// previous step's extrapolated boundary velocity).
+std::vector<std::pair<void*, size_t>> snap_items(Fp32State& st) {
+    const size_t n = st.n;
+    P32& p = st.P[st.cur];
+    std::vector<std::pair<void*, size_t>> v = {
+        {p.hi, sizeof(float4) * n}, {p.lo, sizeof(float4) * n}, {p.vel, sizeof(float4) * n},
+        {p.drho, sizeof(float) * n}, {p.mass, sizeof(float) * n}, {p.ids, sizeof(int4) * n},
+        {st.T.vt, sizeof(float4) * n}};
+    if (p.sig) {
+        v.push_back({p.sig, sizeof(float) * 6 * n});
+        v.push_back({p.eeq, sizeof(float) * n});
+        v.push_back({p.eeqp, sizeof(float) * n});
+        v.push_back({p.flag, sizeof(int) * n});
+    }
+    return v;
+}
+
+int snapshot(Fp32State& st, cudaStream_t s, bool restore) {
+    auto items = snap_items(st);
+    size_t total = 0;
+    for (auto& it : items) total += (it.second + 255) & ~size_t(255);
+    if (!restore && !st.snap && cudaMalloc(&st.snap, total) != cudaSuccess) { st.snap = nullptr; return TSG_E_CUDA; }
+    char* q = static_cast<char*>(st.snap);
+    for (auto& it : items) {
+        if (restore) cudaMemcpyAsync(it.first, q, it.second, cudaMemcpyDeviceToDevice, s);
+        else cudaMemcpyAsync(q, it.first, it.second, cudaMemcpyDeviceToDevice, s);
+        q += (it.second + 255) & ~size_t(255);
+    }
+    return 0;
+}
+
+// Milliseconds per step of `steps` steps from the snapshot state (graph mode).
+float time_steps(Fp32State& st, int steps, bool collide, cudaStream_t s, int* rc) {
+    snapshot(st, s, true);
+    rebuild(st, s, true);
+    *rc = fp32_step_graph(st, 1, collide, s);  // captures the graphs outside the timed region
+    if (st.steps_per_graph > 1 && !*rc) *rc = fp32_step_graph(st, st.steps_per_graph, collide, s);
+    if (*rc) return 1e30f;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+    *rc = fp32_step_graph(st, steps, collide, s);
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return *rc ? 1e30f : ms / steps;
+}
+
+// Milliseconds of one re-sort + list build from the snapshot state.
+float time_rebuild(Fp32State& st, cudaStream_t s) {
+    snapshot(st, s, true);
+    rebuild(st, s, true);  // warm
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+    for (int q = 0; q < 3; ++q) rebuild(st, s, true);
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms / 3.f;
+}
+
+}  // namespace
+
+// Coordinate search over the launch parameters, each candidate timed from the same saved
+// state: threads per block of the neighbour kernels (full steps), cells per CTA of the
+// list build (re-sort + build), steps per graph launch (full steps).  The state is put
+// back afterwards, so tuning does not advance the simulation.
+int fp32_autotune(Fp32State& st, int trial_steps, bool collide, cudaStream_t s, float* ms_out) {
+    if (trial_steps < 1) return TSG_E_ARG;
+    if (profiling_on()) return TSG_E_STATE;
+    if (!st.built) fp32_sort(st, s);
+    fold_rebuilds(st, s);
+    const long long launches0 = launch_total();
+    const long long rebuilds0 = st.rebuilds;
+    int rc = snapshot(st, s, false);
+    if (rc) return rc;
+    const int tpbs[] = {64, 128, 256};
+    const int cpcs3[] = {2, 4, 8}, cpcs2[] = {0, 2, 4, 8};
+    const int spgs[] = {1, 4, 16};
+    float best = 1e30f;
+    int bt = st.tpb;
+    for (int t : tpbs) {
+        st.tpb = t;
+        const float ms = time_steps(st, trial_steps, collide, s, &rc);
+        if (rc) break;
+        if (ms < best) { best = ms; bt = t; }
+    }
+    st.tpb = bt;
+    if (!rc) {
+        float bestr = 1e30f;
+        int bc = st.cells_per_cta;
+        const int* cp = st.k.dim == 3 ? cpcs3 : cpcs2;
+        const int ncp = st.k.dim == 3 ? 3 : 4;
+        for (int q = 0; q < ncp; ++q) {
+            st.cells_per_cta = cp[q];
+            const float ms = time_rebuild(st, s);
+            if (ms < bestr) { bestr = ms; bc = cp[q]; }
+        }
+        st.cells_per_cta = bc;
+    }
+    if (!rc) {
+        int bs = st.steps_per_graph;
+        best = 1e30f;
+        for (int k : spgs) {
+            st.steps_per_graph = k;
+            const float ms = time_steps(st, trial_steps < k ? k : trial_steps, collide, s, &rc);
+            if (rc) break;
+            if (ms < best) { best = ms; bs = k; }
+        }
+        st.steps_per_graph = bs;
+    }
+    snapshot(st, s, true);
+    rebuild(st, s, true);
+    cudaStreamSynchronize(s);
+    cudaFree(st.snap);
+    st.snap = nullptr;
+    // tuning steps are not simulation steps: take their launches and rebuilds back out
+    fold_rebuilds(st, s);
+    add_launches(launches0 - launch_total());
+    st.rebuilds = rebuilds0;
+    if (ms_out) *ms_out = best;
+    return rc ? rc : (cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA);
+}
 
 int fp32_field(Fp32State& st, const char* name, tsg_view* out, cudaStream_t s) {
     const std::string f(name);
@@ -1406,11 +2392,18 @@ int fp32_field(Fp32State& st, const char* name, tsg_view* out, cudaStream_t s) {
         {"x", 0, 3, 0}, {"v", 1, 3, 0}, {"density", 2, 1, 0}, {"pressure", 3, 1, 0}, {"m_V", 4, 1, 0},
         {"mass", 5, 1, 0}, {"v_tmp", 6, 3, 0}, {"density_tmp", 7, 1, 0}, {"d_density", 8, 1, 0},
         {"d_vel", 9, 3, 0}, {"CSPM_f", 10, 1, 0}, {"CSPM_L", 11, 9, 0},
-        {"id0", 0, 1, 1}, {"mat_type", 1, 1, 1}, {"mat_id", 2, 1, 1}, {"obj_id", 3, 1, 1}, {"is_dynamic", 4, 1, 1}};
+        {"stress", 12, 9, 0}, {"stress_tmp", 13, 9, 0}, {"d_stress", 14, 9, 0}, {"strain_equ", 15, 1, 0},
+        {"strain_equ_p", 16, 1, 0}, {"d_strain_equ", 17, 1, 0}, {"d_strain_equ_p", 18, 1, 0},
+        {"id0", 0, 1, 1}, {"mat_type", 1, 1, 1}, {"mat_id", 2, 1, 1}, {"obj_id", 3, 1, 1}, {"is_dynamic", 4, 1, 1},
+        {"flag_retmap", 5, 1, 1}};
     const Spec* sp = nullptr;
     for (const Spec& x : specs) if (f == x.nm) sp = &x;
     if (!sp) return TSG_E_NAME;
     if (sp->what == 11 && !st.T.L) return TSG_E_NAME;
+    const bool soil = st.P[0].sig != nullptr, dp = st.T.dsig != nullptr;
+    if (!sp->is_int && sp->what >= 12 && !soil) return TSG_E_NAME;
+    if (!sp->is_int && (sp->what == 14 || sp->what == 16 || sp->what == 18) && !dp) return TSG_E_NAME;
+    if (sp->is_int && sp->what == 5 && !dp) return TSG_E_NAME;
     double* buf = nullptr;
     for (auto& v : st.views) if (v.first == f) buf = v.second;
     if (!buf) {
@@ -1486,6 +2479,24 @@ int fp32_read(Fp32State& st, const char* name, void* dst, bool to_device, cudaSt
         cudaMemcpyAsync(dst, st.stage, sizeof(double) * n * comps, kind, s);
     }
     if (!to_device) cudaStreamSynchronize(s);
+    return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
+}
+
+}  // namespace tsg
+
+namespace tsg {
+
+int fp32_batch_diag(Fp32State& st, double pitch, double* host_out, int nscenes, cudaStream_t s) {
+    if (st.nscenes <= 0 || nscenes != st.nscenes) return TSG_E_ARG;
+    double* d = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * 8 * (size_t)nscenes) != cudaSuccess) return TSG_E_CUDA;
+    std::vector<double> init(8 * (size_t)nscenes, 0.0);
+    for (int q = 0; q < nscenes; ++q) init[8 * (size_t)q + 7] = -DBL_MAX;
+    cudaMemcpyAsync(d, init.data(), sizeof(double) * init.size(), cudaMemcpyHostToDevice, s);
+    TSG_LAUNCH(k_diag_batch32, nblk(st.nd), TPB, s, st.k, st.P[st.cur], pitch, d);
+    cudaMemcpyAsync(host_out, d, sizeof(double) * init.size(), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    cudaFree(d);
     return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
 }
 

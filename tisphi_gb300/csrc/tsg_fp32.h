@@ -6,8 +6,17 @@ namespace tsg {
 
 struct Fp32State;
 
+// Batched ensemble description (host arrays): scene number per particle and the per-scene
+// Tait stiffness / viscosity factor 2 (d + 2) nu.
+struct Fp32Scenes {
+    const int* scene_of = nullptr;   // n entries
+    const float* stiffness = nullptr;
+    const float* visc_fac = nullptr;
+    int nscenes = 0;
+};
+
 int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* p, bool from_device,
-                Fp32State** out, cudaStream_t s);
+                Fp32State** out, cudaStream_t s, const Fp32Scenes* scenes = nullptr);
 void fp32_destroy(Fp32State* st);
 void fp32_sort(Fp32State& st, cudaStream_t s);
 // True when the neighbour lists must be rebuilt before the next step (always without a skin).
@@ -22,6 +31,23 @@ const int* fp32_cell_start(const Fp32State& st);
 void fp32_neighbors(Fp32State& st, int* counts, int* offsets, int* list, cudaStream_t s);
 void fp32_diag(Fp32State& st, double* scratch, double* host_out8, cudaStream_t s);
 int* fp32_err_ptr(Fp32State& st);
+// out[0] / out[1] list entries stored for the dynamic / static block, out[2] overflowed
+// particles, out[3] list builds since creation.
+int fp32_list_stats(Fp32State& st, int64_t* out4, cudaStream_t s);
+
+// Graph mode: nsteps full steps replayed from captured graphs (the re-sort runs inside the
+// graph when the device-side displacement check asks for it).  TSG_E_STATE while
+// per-phase profiling is on.
+int fp32_step_graph(Fp32State& st, int nsteps, bool collide, cudaStream_t s);
+// Fold device-side rebuild counts of graph replays into the host counters (synchronises).
+void fp32_flush_counters(Fp32State& st, cudaStream_t s);
+void fp32_get_launch(const Fp32State& st, int* tpb, int* cells_per_cta, int* steps_per_graph);
+int fp32_set_launch(Fp32State& st, int tpb, int cells_per_cta, int steps_per_graph);
+// Time launch-parameter candidates from a saved state and keep the fastest; the particle
+// state is restored (re-sorted) afterwards.  *ms_out = best milliseconds per step.
+int fp32_autotune(Fp32State& st, int trial_steps, bool collide, cudaStream_t s, float* ms_out);
+// Per-scene diagnostics of a batched ensemble (host out, 8 values per scene).
+int fp32_batch_diag(Fp32State& st, double pitch, double* host_out, int nscenes, cudaStream_t s);
 int fp32_write(Fp32State& st, const char* name, const void* src, bool from_device, cudaStream_t s);
 int fp32_read(Fp32State& st, const char* name, void* dst, bool to_device, cudaStream_t s);
 

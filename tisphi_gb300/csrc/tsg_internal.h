@@ -7,8 +7,14 @@
 
 namespace tsg {
 
-// Host-side count of kernel launches issued by this library (all handles).
+// Host-side count of kernel launches issued by this library (all handles).  Graph replays
+// add their kernel-node counts through add_launches; launches recorded while a stream is
+// being captured are taken back out (they are nodes, not launches).
 void note_launch();
+void add_launches(long long delta);
+long long launch_total();
+// True while tsg_profile is on (steps then run eagerly, with per-phase events).
+bool profiling_on();
 #define TSG_LAUNCH(kernel, grid, block, stream, ...)                   \
     do {                                                                \
         ::tsg::note_launch();                                           \

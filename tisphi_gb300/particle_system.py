@@ -182,6 +182,14 @@ class ParticleSystem:
         return {"mass": out[0], "momentum": out[1:4].copy(), "kinetic": out[4], "potential": out[5],
                 "vmax": out[6], "front": out[7]}
 
+    def list_stats(self):
+        """FP32-mixed neighbour-list occupancy: entries of real / dummy particles, overflowed
+        particles and list builds since upload (raises for the FP64 form, which keeps no lists)."""
+        out = np.zeros(4, dtype=np.int64)
+        nat.check(self._lib.tsg_list_stats(self._h, nat.as_ptr(out, ctypes.c_int64), _stream()), "list_stats")
+        return {"entries_real": int(out[0]), "entries_dummy": int(out[1]), "overflowed": int(out[2]),
+                "builds": int(out[3])}
+
     def check_errors(self):
         """Raise when the device error word has bits set (synchronises)."""
         rc = self._lib.tsg_last_error(self._h, _stream())

@@ -10,6 +10,10 @@ workloads are:
 * ``dambreak_3d`` - 3D WCSPH dambreak: domain 3.22 x 1.6 x 0.5 m, block 1.2 x 0.6 x 0.2 m,
   spacing 0.0054 m (911,754 fluid + 1,413,114 dummy particles), CSPM correction on, XSPH
   off, leap-frog at dt 2e-5, jitter +-1 % of the spacing.
+* ``dambreak_ensemble`` - B independent 2D dambreaks for a batched run: block width
+  uniform in [0.3, 1.5] m, height uniform in [0.2, 0.8] m, stiffness log-uniform in
+  [2e4, 1e5], viscosity log-uniform in [1e-3, 1e-2], all drawn from one seed (numpy
+  PCG64); spacing 0.01 m, leap-frog at dt 1e-4, domain 3.22 x 1.6 m.
 * ``column_2d`` - 2D granular column collapse (mu(I) or Drucker-Prager): sand rho0 2040,
   c 0, phi 21.9 deg, E 5.84e6, nu 0.3, psi 0; column 0.2 x 0.1 m at spacing 0.001 m,
   symplectic Euler at dt 1e-5, jitter +-1 % of the spacing.
@@ -78,3 +82,22 @@ def column_2d(method=3, spacing=0.001, dt=1e-5, jitter_frac=0.01, seed=3, integr
         "Materials": [sand()],
         "Blocks": [block((width, height, 0.05))],
     }
+
+
+def dambreak_ensemble(n=256, seed=7, spacing=0.01, dt=1e-4, width=(0.3, 1.5), height=(0.2, 0.8),
+                      stiffness=(2e4, 1e5), viscosity=(1e-3, 1e-2), domain=(3.22, 1.6), jitter=1e-4):
+    """Scene dicts of an ensemble of 2D dambreaks with seeded block sizes and fluid parameters."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for q in range(n):
+        w = float(rng.uniform(*width))
+        hgt = float(rng.uniform(*height))
+        b = float(np.exp(rng.uniform(np.log(stiffness[0]), np.log(stiffness[1]))))
+        nu = float(np.exp(rng.uniform(np.log(viscosity[0]), np.log(viscosity[1]))))
+        # whole lattice rows / columns, as the reference's generator fills the block
+        w = round(w / spacing) * spacing
+        hgt = round(hgt / spacing) * spacing
+        out.append(dambreak_2d(spacing=spacing, width=w, height=hgt, dt=dt, jitter=jitter, seed=seed * 100003 + q,
+                               stiffness=b, viscosity=nu, domain=domain))
+    return out
