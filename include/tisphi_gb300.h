@@ -281,6 +281,35 @@ int tsg_batch_diag(tsg_handle* h, double* out, int32_t nscenes, void* stream);
 /* x shift between consecutive scenes of a batch (0 for an ordinary handle). */
 double tsg_batch_pitch(const tsg_handle* h);
 
+/* Granular material parameters of a created handle: friction angle (rad) and cohesion
+ * (Pa), with the solver constructor's derived constants recomputed (mu = tan(friction) for
+ * mu(I), eng/solver_sph_muI.py:20; alpha, k_c for Drucker-Prager,
+ * eng/solver_sph_dp.py:20-27).  No reference counterpart: the reference fixes them at
+ * construction; the differentiable rollout perturbs them. */
+int tsg_set_soil(tsg_handle* h, double friction, double cohesion);
+
+/* Bitwise snapshots of the FP32-mixed particle state (every per-particle array that
+ * carries from one step to the next, in the current particle order) into / from a device
+ * buffer of tsg_snapshot_bytes(h) bytes.  After a load the next step re-sorts first, so
+ * stepping on from a loaded snapshot repeats the original steps bit for bit.  No
+ * reference counterpart (checkpointing for the adjoint). */
+int64_t tsg_snapshot_bytes(tsg_handle* h);
+int tsg_snapshot_save(tsg_handle* h, void* dst, void* stream);
+int tsg_snapshot_load(tsg_handle* h, const void* src, void* stream);
+
+/* Hand-written adjoint of one FP32-mixed mu(I) step (2D, symplectic Euler, no kernel
+ * correction, dummy boundary, no XSPH; no reference counterpart - the reference's Taichi
+ * kernels are not differentiated).  Call with the state loaded from the snapshot taken
+ * before the step: it repeats the step's forward, then reverses it.  The adjoint arrays
+ * are device f64 arrays in particle-id (id0) order, row-major: adj_x, adj_v, adj_v_tmp
+ * (n, 3), adj_density (n,).  On entry they hold the adjoint of the state after the step
+ * (x, v, density of soil particles; v_tmp of dummy particles, which the next step reads),
+ * on return the adjoint of the state before it.  adj_params (device, 2 doubles) accumulates
+ * d/d mu and d/d cohesion (mu = tan(friction)).  TSG_E_CAPACITY if a neighbour list
+ * overflowed. */
+int tsg_adjoint_step(tsg_handle* h, double* adj_x, double* adj_v, double* adj_density, double* adj_v_tmp,
+                     double* adj_params, void* stream);
+
 /* Human-readable text for a status code. */
 const char* tsg_status_string(int status);
 

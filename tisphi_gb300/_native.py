@@ -74,6 +74,12 @@ SYMBOLS = {
     "tsg_reduce_diag": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "tsg_list_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p]),
     "tsg_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "tsg_set_soil": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]),
+    "tsg_snapshot_bytes": (ctypes.c_int64, [ctypes.c_void_p]),
+    "tsg_snapshot_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "tsg_snapshot_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "tsg_adjoint_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "tsg_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "tsg_get_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "tsg_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, _dp, ctypes.c_void_p]),

@@ -23,6 +23,7 @@ UNITS = {
     "tsg_sort.cu": ["-fmad=false"],
     "tsg_fp64.cu": ["-fmad=false"],
     "tsg_fp32.cu": [],
+    "tsg_adjoint.cu": [],
     "tsg_noalloc.cu": ["-fmad=false"],
 }
 

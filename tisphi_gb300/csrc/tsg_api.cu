@@ -681,6 +681,56 @@ int tsg_last_error(tsg_handle* h, void* stream) {
     return e ? e : v;
 }
 
+int tsg_set_soil(tsg_handle* h, double friction, double cohesion) {
+    if (!h) return TSG_E_ARG;
+    Consts& c = h->c;
+    if (c.solver != 2 && c.solver != 3) return TSG_E_UNSUPPORTED;
+    h->cfg.friction = friction;
+    h->cfg.cohesion = cohesion;
+    c.coh = cohesion;
+    if (c.solver == 2) {
+        c.mu = std::tan(friction);
+    } else {  // the DP constructor's constants (eng/solver_sph_dp.py:20-27)
+        double tf = std::tan(friction);
+        double den = std::sqrt(9 + 12 * std::pow(tf, 2.0));
+        c.alpha = tf / den;
+        c.k_c = 3 * cohesion / den;
+        c.kc_over_alpha = c.k_c / c.alpha;
+        c.lam_den = 27.0 * c.alpha * c.Km * c.sin_dila + c.Gm;
+        c.three_aK = 3.0 * c.alpha * c.Km;
+    }
+    if (use_fp32(h)) fp32_set_soil(*h->f32, c);
+    return 0;
+}
+
+int64_t tsg_snapshot_bytes(tsg_handle* h) {
+    if (!h || !h->uploaded || !use_fp32(h)) return 0;
+    return (int64_t)fp32_snapshot_bytes(*h->f32);
+}
+
+int tsg_snapshot_save(tsg_handle* h, void* dst, void* stream) {
+    if (!h || !h->uploaded) return TSG_E_STATE;
+    if (!use_fp32(h)) return TSG_E_UNSUPPORTED;
+    return fp32_snapshot_copy(*h->f32, dst, false, S(stream));
+}
+
+int tsg_snapshot_load(tsg_handle* h, const void* src, void* stream) {
+    if (!h || !h->uploaded) return TSG_E_STATE;
+    if (!use_fp32(h)) return TSG_E_UNSUPPORTED;
+    return fp32_snapshot_copy(*h->f32, const_cast<void*>(src), true, S(stream));
+}
+
+int tsg_adjoint_step(tsg_handle* h, double* adj_x, double* adj_v, double* adj_density, double* adj_v_tmp,
+                     double* adj_params, void* stream) {
+    if (!h || !h->uploaded) return TSG_E_STATE;
+    if (!adj_x || !adj_v || !adj_density || !adj_v_tmp || !adj_params) return TSG_E_ARG;
+    if (!use_fp32(h)) return TSG_E_UNSUPPORTED;
+    int rc = fp32_adjoint_step(*h->f32, adj_x, adj_v, adj_density, adj_v_tmp, adj_params, S(stream));
+    if (rc) return rc;
+    h->sorted = true;
+    return check_cuda();
+}
+
 int tsg_set_launch(tsg_handle* h, const tsg_launch_cfg* cfg) {
     if (!h || !cfg) return TSG_E_ARG;
     if (!use_fp32(h)) return TSG_E_UNSUPPORTED;

@@ -25,240 +25,13 @@
 //
 // Reference: eng/particle_system.py:228-269 (cell list), eng/solver_sph_base.py:41-238,
 // :363-423, :648-669 (step, CSPM, boundary), eng/solver_sph_wc.py:82-132 (WCSPH).
-#include <cfloat>
-#include <cmath>
-#include <cstring>
-#include <string>
-#include <vector>
-
-#include "tsg_fp32.h"
+#include "tsg_fp32_dev.cuh"
 
 namespace tsg {
 
+using namespace f32;
+
 namespace {
-
-constexpr int TPB = 128;
-inline int nblk(long long n, int tpb = TPB) { return (int)((n + tpb - 1) / tpb); }
-
-struct K32 {
-    int n, nd, dim, kernel, corr, xsph, boundary, solver, maxn, exponent_is_int, gamma_i;
-    int gnum[3];
-    long long G;
-    double vs[3], grid;
-    float Q, inv_grid, h1, kk, kk6, wgrad, cub1, cub2, R2, R2lo, R2hi, pf_lim;
-    float R2L, R2Lhi, disp2_limit;  // list radius (support + skin) and rebuild threshold
-    float visc_fac, eps_h2, rho0, B, gamma, dt, hdt, g[3], rep_fac, diam, h075, r_eps;
-    float ds[3], de[3];
-    // granular solvers (mu(I): mu, c2, coh; Drucker-Prager: alpha ... twoG; both: damping)
-    float mu, c2, coh, alpha, k_c, kc_over_alpha, Gm, Km, sin_dila, lam_den, three_aK, nine_K_sin, twoG;
-    float damp_eps, damp_E, h2;
-    // batched ensembles: per-scene (stiffness B, viscosity factor), indexed by the scene
-    // number in the type word; nullptr for a single scene (B and visc_fac above)
-    const float2* scene_par;
-};
-
-// Type word (the w lane of lo): bits 0-15 material type (signed), bit 16 is_dynamic, bits
-// 17-28 scene number of a batched ensemble, bit 30 set (the word stays a normal float).
-__device__ __forceinline__ int tf_type(float w) { return (int)(short)(__float_as_int(w) & 0xffff); }
-__device__ __forceinline__ int tf_dyn(float w) { return (__float_as_int(w) >> 16) & 1; }
-__device__ __forceinline__ int tf_scene(float w) { return (__float_as_int(w) >> 17) & 0xfff; }
-constexpr int kMaxScenes = 4096;
-__device__ __forceinline__ bool is_flow(int t) { return t == MAT_FLUID || t == MAT_SOIL; }
-
-// Block-compensated accumulator: plain partial sums, Kahan-folded every flush.
-struct CSum {
-    float s = 0.f, c = 0.f, p = 0.f;
-    __device__ __forceinline__ void add(float x) { p += x; }
-    __device__ __forceinline__ void flush() {
-        float y = p - c;
-        float t = s + y;
-        c = (t - s) - y;
-        s = t;
-        p = 0.f;
-    }
-    __device__ __forceinline__ float get() { flush(); return s; }
-};
-
-__device__ __forceinline__ void atomic_max_d(double* addr, double v) {
-    unsigned long long* a = reinterpret_cast<unsigned long long*>(addr);
-    unsigned long long old = *a;
-    while (__longlong_as_double(old) < v) {
-        unsigned long long prev = atomicCAS(a, old, __double_as_longlong(v));
-        if (prev == old) break;
-        old = prev;
-    }
-}
-
-// Cell coordinate trunc((hi + lo) / grid) with the f64 semantics of the reference's cast:
-// an f32 estimate decides unless it lies within its error bound (1e-3 + |t| 2^-20, well
-// above the three roundings of the f32 estimate) of an integer, where f64 decides.
-__device__ __forceinline__ long long cell_coord(const K32& k, float hi, float lo, bool& ok) {
-    const float tf = (hi + lo) * k.inv_grid;
-    const float fr = fabsf(tf - truncf(tf));
-    const float margin = 1e-3f + fabsf(tf) * 9.5367431640625e-7f;
-    if (fabsf(tf) < 1.0e6f && fr > margin && fr < 1.f - margin) return (long long)(int)tf;
-    const double t = ((double)hi + (double)lo) / k.grid;
-    if (!(fabs(t) < 2147483647.0)) { ok = false; return 0; }
-    return (long long)(int)t;
-}
-
-// |x| from |x|^2 through the hardware reciprocal square root (~2 ulp; 0 -> NaN, which the
-// kernel functions' support test rejects).
-__device__ __forceinline__ float fast_sqrt(float r2) { return r2 * rsqrtf(r2); }
-
-// Kernel value and gradient factor: W(r) and G with grad W = G * dx.
-__device__ __forceinline__ float w_val(const K32& k, float r) {
-    float q = r * k.h1;
-    if (!(r > 1e-8f && q <= 2.f)) return 0.f;
-    if (k.kernel == 1) {
-        float q1 = 1.f - 0.5f * q;
-        float q2 = q1 * q1;
-        return k.kk * (q2 * q2) * (1.f + 2.f * q);
-    }
-    if (q <= 1.f) return k.kk * ((0.5f * q - 1.f) * q * q + 2.f / 3.f);
-    float t = 2.f - q;
-    return k.kk6 * t * t * t;
-}
-__device__ __forceinline__ float w_grad(const K32& k, float r) {
-    float q = r * k.h1;
-    if (!(r > 1e-8f && q <= 2.f)) return 0.f;
-    if (k.kernel == 1) {
-        float q1 = 1.f - 0.5f * q;
-        return k.wgrad * (q1 * q1 * q1);                // -5 k h1^2 q1^3
-    }
-    const float inv = __fdividef(1.f, r);
-    if (q <= 1.f) return k.cub1 * q * (1.5f * q - 2.f) * inv;   // k h1 q (1.5 q - 2) / r
-    float f = 2.f - q;
-    return k.cub2 * f * f * inv;                       // -0.5 k h1 f^2 / r
-}
-
-template <int DIM>
-__device__ __forceinline__ void delta(const float4& hi_i, const float4& lo_i, const float4& hi_j, const float4& lo_j,
-                                      float* d) {
-    d[0] = (hi_i.x - hi_j.x) + (lo_i.x - lo_j.x);
-    d[1] = (hi_i.y - hi_j.y) + (lo_i.y - lo_j.y);
-    d[2] = DIM == 3 ? (hi_i.z - hi_j.z) + (lo_i.z - lo_j.z) : 0.f;
-}
-
-// Candidate enumeration over the stencil of i (reference traversal order of cells, dynamic
-// block first, then the static block for flow centres).  body(j, d, r2) gets the exact
-// f32 displacement x_i - x_j.  The cheap prefilter compares the positions of the last list
-// build (PF): with a skin, particles have moved at most 0.45 skin since then while the
-// lists are in use, so a build-time distance above (R + skin)(1 + 2^-11) rules a pair out
-// for the current positions as well.  Callers after advect_pos (positions moved past the
-// last check) pass use_pf = false.
-template <int DIM, class F>
-__device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4* __restrict__ HI,
-                                               const float4* __restrict__ LO, const float4* __restrict__ PF,
-                                               const int* __restrict__ dstart, const int* __restrict__ sstart,
-                                               bool flow_i, F&& body, bool list_radius = false,
-                                               bool use_pf = true) {
-    const float cut2 = list_radius ? k.R2L : k.R2;
-    const float cut2hi = k.R2Lhi;
-    const float4 hi_i = HI[i], lo_i = LO[i], pf_i = PF[i];
-    bool ok = true;
-    const long long cc0 = cell_coord(k, hi_i.x, lo_i.x, ok);
-    const long long cc1 = cell_coord(k, hi_i.y, lo_i.y, ok);
-    const long long cc2 = cell_coord(k, hi_i.z, lo_i.z, ok);
-    if (!ok) return;
-    const bool pf = use_pf && fabsf(pf_i.x) < k.pf_lim && fabsf(pf_i.y) < k.pf_lim && fabsf(pf_i.z) < k.pf_lim;
-    const long long ny = k.gnum[1], nz = k.gnum[2], G = k.G;
-    for (int blk = 0; blk < (flow_i ? 2 : 1); ++blk) {
-        const int* cs = blk == 0 ? dstart : sstart;
-#pragma unroll 1
-        for (int ox = -1; ox <= 1; ++ox) {
-#pragma unroll 1
-            for (int oy = (DIM == 3 ? -1 : 0); oy <= (DIM == 3 ? 1 : 0); ++oy) {
-                long long f0 = (cc0 + ox) * ny * nz + (cc1 + oy) * nz + cc2;
-                long long lo = f0 - 1 > 0 ? f0 - 1 : 0;
-                long long hi = f0 + 1 < G - 1 ? f0 + 1 : G - 1;
-                if (lo > hi) continue;
-                const int jb = cs[lo], je = cs[hi + 1];
-#pragma unroll 2
-                for (int j = jb; j < je; ++j) {
-                    if (j == i) continue;
-                    const float4 pj = PF[j];
-                    if (!flow_i && !is_flow(tf_type(pj.w))) continue;
-                    float r2f;
-                    if (pf) {
-                        float fx = pf_i.x - pj.x, fy = pf_i.y - pj.y, fz = pf_i.z - pj.z;
-                        r2f = fx * fx + fy * fy;
-                        if (DIM == 3) r2f += fz * fz;
-                        if (r2f > cut2hi) continue;
-                    }
-                    float d[3];
-                    delta<DIM>(hi_i, lo_i, HI[j], LO[j], d);
-                    float r2 = d[0] * d[0] + d[1] * d[1];
-                    if (DIM == 3) r2 += d[2] * d[2];
-                    if (!(r2 < cut2)) continue;
-                    body(j, d, r2);
-                }
-            }
-        }
-    }
-}
-
-// Iterate i's neighbour list (FB = false) or traverse its stencil directly (FB = true: the
-// particle's list overflowed).  The next list index is fetched one iteration ahead.
-template <int DIM, bool FB, class F>
-__device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
-                                         const float4* __restrict__ HI, const float4* __restrict__ LO,
-                                         const float4* __restrict__ PF, const int* __restrict__ dstart,
-                                         const int* __restrict__ sstart, bool flow_i, F&& body) {
-    if (!FB) {
-        const int m = cnt[i];
-        const float4 hi_i = HI[i], lo_i = LO[i];
-        const size_t stride = (size_t)k.n;
-        const int* lp = nbr + i;
-        // two neighbours per trip: both index loads, then both position loads, then compute
-        int s = 0;
-        for (; s + 1 < m; s += 2) {
-            const int j0 = lp[0], j1 = lp[stride];
-            lp += 2 * stride;
-            const float4 h0 = HI[j0], l0 = LO[j0], h1 = HI[j1], l1 = LO[j1];
-            float d0[3], d1[3];
-            delta<DIM>(hi_i, lo_i, h0, l0, d0);
-            delta<DIM>(hi_i, lo_i, h1, l1, d1);
-            float r20 = d0[0] * d0[0] + d0[1] * d0[1];
-            float r21 = d1[0] * d1[0] + d1[1] * d1[1];
-            if (DIM == 3) { r20 += d0[2] * d0[2]; r21 += d1[2] * d1[2]; }
-            if (r20 < k.R2) body(j0, d0, r20, s);        // lists hold support + skin
-            if (r21 < k.R2) body(j1, d1, r21, s + 1);
-        }
-        if (s < m) {
-            const int j = lp[0];
-            float d[3];
-            delta<DIM>(hi_i, lo_i, HI[j], LO[j], d);
-            float r2 = d[0] * d[0] + d[1] * d[1];
-            if (DIM == 3) r2 += d[2] * d[2];
-            if (r2 < k.R2) body(j, d, r2, s);
-        }
-    } else {
-        int s = 0;
-        enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i,
-                            [&](int j, const float* d, float r2) { body(j, d, r2, s++); });
-    }
-}
-
-// Particle loop shared by the list kernels (FB = false: one particle per thread, skipping
-// overflowed lists) and their overflow passes (FB = true: grid-stride over the overflow list).
-struct Ovf {
-    const int* list;
-    const int* count;
-};
-#define FOR_PARTICLES(FB, BASE, N, OVF, CNT, MAXN, ...)                                         \
-    do {                                                                                        \
-        if (!(FB)) {                                                                            \
-            const int i = (BASE) + blockIdx.x * blockDim.x + threadIdx.x;                       \
-            if (i < (N) && (CNT)[i] <= (MAXN)) { __VA_ARGS__ }                                  \
-        } else {                                                                                \
-            const int no = *(OVF).count;                                                        \
-            for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < no; q += gridDim.x * blockDim.x) { \
-                const int i = (OVF).list[q];                                                    \
-                if (i >= (BASE) && i < (N)) { __VA_ARGS__ }                                     \
-            }                                                                                   \
-        }                                                                                       \
-    } while (0)
 
 // ---------------------------------------------------------------- sort (dynamic block)
 __global__ void k_hash32(K32 k, int count_n, int base, const float4* __restrict__ HI, const float4* __restrict__ LO,
@@ -299,24 +72,6 @@ __global__ void k_cell_sort32(long long ncell, const int* __restrict__ cell_star
         perm[m + 1] = v;
     }
 }
-
-// Persistent per-particle state of the FP32-mixed form.
-struct P32 {
-    float4* hi;     // (hx, hy, hz, m_V)
-    float4* lo;     // (lx, ly, lz, type word)
-    float4* vel;    // (vx, vy, vz, pressure)
-    float* drho;    // density - rho0
-    float* mass;
-    int4* ids;      // (id0, mat_id, obj_id, is_dynamic)
-    // granular solvers only (nullptr for WCSPH)
-    float* sig;     // stress, 6 planes of n (symmetric: xx, yy, zz, xy, xz, yz)
-    float* eeq;     // equivalent strain
-    float* eeqp;    // equivalent plastic strain (Drucker-Prager)
-    int* flag;      // return-mapping case (Drucker-Prager)
-};
-
-// Symmetric 3x3 tensors are stored as six planes: xx, yy, zz, xy, xz, yz.
-__device__ __forceinline__ int sym_idx(int a, int b) { return a == b ? a : 2 + a + b; }
 
 // Gather block [base, base + count_n) from a into b (new order), renormalise hi/lo and
 // refresh the prefilter position.
@@ -525,25 +280,6 @@ __global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float
     }
 }
 
-// ---------------------------------------------------------------- transient state
-struct T32 {
-    float4* vt;     // (v_tmp, p / rho_tmp^2)
-    float2* pr;     // (pressure, rho_tmp)
-    float* drt;     // rho_tmp - rho0
-    float* dd;      // d_density
-    float4* dv;     // d_vel
-    float* cf;      // CSPM_f
-    float* L;       // CSPM_L, 9 planes
-    float4* xs;     // XSPH sums
-    int* cnt;
-    int* nbr;
-    // granular solvers only
-    float* sigt;    // stress_tmp, 6 planes
-    float* dsig;    // d_stress, 6 planes (Drucker-Prager)
-    float* dee;     // d_strain_equ
-    float* deep;    // d_strain_equ_p (Drucker-Prager)
-};
-
 template <int DIM>
 __device__ __forceinline__ void inv_store(const K32& k, float* L, int i, const double* m, bool flow_i) {
     double inv[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
@@ -747,47 +483,6 @@ __global__ void k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, co
     });
 }
 
-// ---------------------------------------------------------------- granular solvers
-// Drucker-Prager invariants and stress adaptation (eng/solver_sph_dp.py:42-109) on the
-// six stored components; s:s counts each off-diagonal entry twice.
-__device__ __forceinline__ void dp_inv32(const K32& k, const float* st, float* s, float& I1, float& sJ2, float& f) {
-    const float tr = (st[0] + st[1]) + st[2];
-    const float t3 = tr / 3.f;
-    s[0] = st[0] - t3; s[1] = st[1] - t3; s[2] = st[2] - t3;
-    s[3] = st[3]; s[4] = st[4]; s[5] = st[5];
-    I1 = tr;
-    const float ss = s[0] * s[0] + s[1] * s[1] + s[2] * s[2] + 2.f * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
-    sJ2 = sqrtf(0.5f * ss);
-    f = sJ2 + k.alpha * I1 - k.k_c;
-}
-__device__ __forceinline__ void dp_adapt32(const K32& k, float* st) {
-    float s[6], I1, sJ2, f;
-    dp_inv32(k, st, s, I1, sJ2, f);
-    if (f > (float)EPS_F) {
-        if (f > sJ2) {
-            const float tt = (I1 - k.kc_over_alpha) / 3.f;
-            st[0] -= tt; st[1] -= tt; st[2] -= tt;
-        }
-        dp_inv32(k, st, s, I1, sJ2, f);
-        const float r = (-I1 * k.alpha + k.k_c) / sJ2;
-        for (int q = 0; q < 6; ++q) st[q] = r * s[q] + (q < 3 ? I1 / 3.f : 0.f);
-    }
-}
-__device__ __forceinline__ int dp_flag32(const K32& k, const float* st) {
-    float s[6], I1, sJ2, f;
-    dp_inv32(k, st, s, I1, sJ2, f);
-    if (f < -(float)EPS_F) return 0;
-    if (f > (float)EPS_F) return f >= sJ2 ? 3 : 2;
-    return 1;
-}
-
-__device__ __forceinline__ void load_sym(const float* __restrict__ a, size_t n, int i, float* out) {
-    for (int q = 0; q < 6; ++q) out[q] = a[q * n + i];
-}
-__device__ __forceinline__ void store_sym(float* __restrict__ a, size_t n, int i, const float* v) {
-    for (int q = 0; q < 6; ++q) a[q * n + i] = v[q];
-}
-
 // Drucker-Prager first phase of one_step: adapt stress_tmp (eng/solver_sph_dp.py:215-217).
 __global__ void k_pre_dp32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -797,45 +492,6 @@ __global__ void k_pre_dp32(K32 k, P32 p, T32 t) {
     load_sym(t.sigt, k.n, i, st);
     dp_adapt32(k, st);
     store_sym(t.sigt, k.n, i, st);
-}
-
-// Corrected kernel gradient L (G d) (or G d when CORR is off).
-template <int DIM, bool CORR>
-__device__ __forceinline__ void grad_c(const float* L, float gf, const float* d, float* kc) {
-    const float gx = gf * d[0], gy = gf * d[1], gz = DIM == 3 ? gf * d[2] : 0.f;
-    if (CORR) {
-        kc[0] = L[0] * gx + L[1] * gy + (DIM == 3 ? L[2] * gz : 0.f);
-        kc[1] = L[3] * gx + L[4] * gy + (DIM == 3 ? L[5] * gz : 0.f);
-        kc[2] = DIM == 3 ? L[6] * gx + L[7] * gy + L[8] * gz : 0.f;
-    } else {
-        kc[0] = gx; kc[1] = gy; kc[2] = gz;
-    }
-}
-
-// Velocity gradient sum_j m_Vj (v_j - v_i) (x) kc and continuity sum_j m_Vj (v_i - v_j) . kc.
-template <int DIM>
-__device__ __forceinline__ void vgrad_add(float mVj, const float4& vti, const float4& vtj, const float* kc, float* vg,
-                                          CSum& dd) {
-    const float u[3] = {mVj * (vtj.x - vti.x), mVj * (vtj.y - vti.y), DIM == 3 ? mVj * (vtj.z - vti.z) : 0.f};
-#pragma unroll
-    for (int a = 0; a < DIM; ++a)
-#pragma unroll
-        for (int b = 0; b < DIM; ++b) vg[3 * a + b] += u[a] * kc[b];
-    dd.add(-(u[0] * kc[0] + u[1] * kc[1] + (DIM == 3 ? u[2] * kc[2] : 0.f)));
-}
-
-// Symmetric / antisymmetric parts of a full velocity gradient.
-__device__ __forceinline__ void strain_rate(const float* vg, float* er) {
-    er[0] = vg[0]; er[1] = vg[4]; er[2] = vg[8];
-    er[3] = 0.5f * (vg[1] + vg[3]); er[4] = 0.5f * (vg[2] + vg[6]); er[5] = 0.5f * (vg[5] + vg[7]);
-}
-__device__ __forceinline__ float sym_dd(const float* a, const float* b) {
-    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + 2.f * (a[3] * b[3] + a[4] * b[4] + a[5] * b[5]);
-}
-__device__ __forceinline__ float equiv_rate(const float* er) {  // sqrt(2/3 dev(e):dev(e))
-    const float t3 = ((er[0] + er[1]) + er[2]) / 3.f;
-    float ed[6] = {er[0] - t3, er[1] - t3, er[2] - t3, er[3], er[4], er[5]};
-    return sqrtf(sym_dd(ed, ed) * 2.f / 3.f);
 }
 
 // mu(I) loop 1 (eng/solver_sph_muI.py:67-92): velocity gradient, continuity, pressure from
@@ -1534,45 +1190,6 @@ __global__ void k_set_rebuild32(cudaGraphConditionalHandle hnd, const unsigned* 
 
 }  // namespace
 
-// ====================================================================== host side
-struct Fp32State {
-    K32 k{};
-    Consts c{};
-    int n = 0, nd = 0;
-    P32 P[2]{};
-    int cur = 0;
-    T32 T{};
-    float4* pf = nullptr;
-    int *dcount = nullptr, *dstart = nullptr, *scount = nullptr, *sstart = nullptr;
-    int *cell_of = nullptr, *rank = nullptr, *perm = nullptr, *tiles = nullptr, *err = nullptr;
-    int *cells_d = nullptr, *cells_s = nullptr, *ncells = nullptr;  // non-empty cells (dynamic, static)
-    int *ovf_list = nullptr, *novf = nullptr;  // particles whose neighbours exceed the list capacity
-    unsigned* maxdisp = nullptr;               // squared displacement since the last list build
-    bool built = false;
-    double* stage = nullptr;       // f64 export staging (9 n)
-    double* scratch = nullptr;
-    std::vector<void*> allocs;
-    std::vector<std::pair<std::string, double*>> views;
-    bool lists_valid = false;
-    long long rebuilds = 0;        // list builds since creation
-    int nscenes = 0;               // > 0 for a batched ensemble
-    // launch configuration (tsg_set_launch / tsg_autotune): threads per block of the
-    // neighbour kernels, cells per CTA of the warp-per-cell list build (0: one thread per
-    // particle), steps per captured graph
-    int tpb = 128, cells_per_cta = 4, steps_per_graph = 1;
-    // captured step graphs: [0] one step, [1] steps_per_graph steps
-    struct StepGraph {
-        cudaGraphExec_t exec = nullptr;
-        int steps = 0, cur = -1, tpb = 0, cpc = 0;
-        bool collide = false;
-        long long kernels = 0;    // kernel nodes outside the conditional rebuild bodies
-    } graphs[2];
-    long long body_kernels = 0;   // kernel nodes of one rebuild body
-    int* d_rebuilds = nullptr;    // rebuilds taken by graph replays (device counter)
-    int rebuilds_seen = 0;        // part of d_rebuilds already folded into the counters
-    void* snap = nullptr;         // autotuner snapshot of the particle state
-};
-
 namespace {
 
 template <class T>
@@ -1831,6 +1448,7 @@ void fp32_destroy(Fp32State* st) {
     for (auto& g : st->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     if (st->snap) cudaFree(st->snap);
+    fp32_free_adjoint(*st);
     for (void* p : st->allocs) cudaFree(p);
     delete st;
 }
@@ -1891,9 +1509,11 @@ __global__ void k_copy_back32(int nd, P32 b, P32 a, size_t n) {
     }
 }
 
+}  // namespace
+
 // Re-sort the dynamic block and rebuild every list.  in_place keeps the current buffer
 // (the sorted block is copied back), as a captured graph needs fixed pointers.
-void rebuild(Fp32State& st, cudaStream_t s, bool in_place) {
+void f32::rebuild(Fp32State& st, cudaStream_t s, bool in_place) {
     {
         PhaseScope ph(s, PH_SORT);
         if (st.nd > 0) {
@@ -1911,8 +1531,6 @@ void rebuild(Fp32State& st, cudaStream_t s, bool in_place) {
     }
     cudaMemsetAsync(st.maxdisp, 0, sizeof(unsigned), s);
 }
-
-}  // namespace
 
 void fp32_sort(Fp32State& st, cudaStream_t s) {
     rebuild(st, s, false);
@@ -2095,12 +1713,10 @@ void fp32_advect(Fp32State& st, int which, cudaStream_t s) {
 void fp32_rk_update(Fp32State&, int, cudaStream_t) {}
 
 // ---------------------------------------------------------------- captured steps
-namespace {
-
 // One SPHBase.step() after the (conditional) re-sort: kernel correction, init_real2tmp,
 // the integrator's one_step / advect sequence, advect_pos, advect_something and, in
 // collision mode, enforce_boundary (eng/solver_sph_base.py:41-61, :79-120).
-void step_body(Fp32State& st, cudaStream_t s, bool collide) {
+void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
     fp32_kernel_corr(st, s);
     fp32_init_tmp(st, s);
     fp32_one_step(st, s);
@@ -2113,6 +1729,8 @@ void step_body(Fp32State& st, cudaStream_t s, bool collide) {
     fp32_advect(st, TSG_ADVECT_SOMETHING, s);
     if (collide) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
 }
+
+namespace {
 
 // Fold the device rebuild counter into the host counters (synchronises s).
 void fold_rebuilds(Fp32State& st, cudaStream_t s) {
@@ -2269,17 +1887,27 @@ std::vector<std::pair<void*, size_t>> snap_items(Fp32State& st) {
     return v;
 }
 
-int snapshot(Fp32State& st, cudaStream_t s, bool restore) {
-    auto items = snap_items(st);
+size_t snap_bytes(Fp32State& st) {
     size_t total = 0;
-    for (auto& it : items) total += (it.second + 255) & ~size_t(255);
-    if (!restore && !st.snap && cudaMalloc(&st.snap, total) != cudaSuccess) { st.snap = nullptr; return TSG_E_CUDA; }
-    char* q = static_cast<char*>(st.snap);
-    for (auto& it : items) {
+    for (auto& it : snap_items(st)) total += (it.second + 255) & ~size_t(255);
+    return total;
+}
+
+void snap_copy(Fp32State& st, void* buf, bool restore, cudaStream_t s) {
+    char* q = static_cast<char*>(buf);
+    for (auto& it : snap_items(st)) {
         if (restore) cudaMemcpyAsync(it.first, q, it.second, cudaMemcpyDeviceToDevice, s);
         else cudaMemcpyAsync(q, it.first, it.second, cudaMemcpyDeviceToDevice, s);
         q += (it.second + 255) & ~size_t(255);
     }
+}
+
+int snapshot(Fp32State& st, cudaStream_t s, bool restore) {
+    if (!restore && !st.snap && cudaMalloc(&st.snap, snap_bytes(st)) != cudaSuccess) {
+        st.snap = nullptr;
+        return TSG_E_CUDA;
+    }
+    snap_copy(st, st.snap, restore, s);
     return 0;
 }
 
@@ -2323,6 +1951,26 @@ float time_rebuild(Fp32State& st, cudaStream_t s) {
 }
 
 }  // namespace
+
+size_t fp32_snapshot_bytes(Fp32State& st) { return snap_bytes(st); }
+
+int fp32_snapshot_copy(Fp32State& st, void* buf, bool load, cudaStream_t s) {
+    if (!buf) return TSG_E_ARG;
+    snap_copy(st, buf, load, s);
+    if (load) {
+        st.built = false;  // the next step re-sorts the loaded particles before anything else
+        st.lists_valid = false;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
+}
+
+void fp32_set_soil(Fp32State& st, const Consts& c) {
+    K32& k = st.k;
+    k.mu = (float)c.mu; k.coh = (float)c.coh; k.alpha = (float)c.alpha; k.k_c = (float)c.k_c;
+    k.kc_over_alpha = (float)c.kc_over_alpha; k.lam_den = (float)c.lam_den; k.three_aK = (float)c.three_aK;
+    for (auto& g : st.graphs)
+        if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+}
 
 // Coordinate search over the launch parameters, each candidate timed from the same saved
 // state: threads per block of the neighbour kernels (full steps), cells per CTA of the

@@ -46,6 +46,17 @@ int fp32_set_launch(Fp32State& st, int tpb, int cells_per_cta, int steps_per_gra
 // Time launch-parameter candidates from a saved state and keep the fastest; the particle
 // state is restored (re-sorted) afterwards.  *ms_out = best milliseconds per step.
 int fp32_autotune(Fp32State& st, int trial_steps, bool collide, cudaStream_t s, float* ms_out);
+// Bitwise snapshot of the particle state in the current particle order (device buffer of
+// fp32_snapshot_bytes bytes): load marks the lists stale, so the next step re-sorts first.
+size_t fp32_snapshot_bytes(Fp32State& st);
+int fp32_snapshot_copy(Fp32State& st, void* buf, bool load, cudaStream_t s);
+// Replace the granular material constants (mu(I): tan(friction), cohesion; Drucker-Prager:
+// the yield-surface constants) of a created state; captured graphs are dropped.
+void fp32_set_soil(Fp32State& st, const Consts& c);
+// Adjoint of one mu(I) symplectic-Euler step from the loaded state (tsg_adjoint.cu).
+int fp32_adjoint_step(Fp32State& st, double* ax, double* av, double* ar, double* avt, double* pbar,
+                      cudaStream_t s);
+void fp32_free_adjoint(Fp32State& st);
 // Per-scene diagnostics of a batched ensemble (host out, 8 values per scene).
 int fp32_batch_diag(Fp32State& st, double pitch, double* host_out, int nscenes, cudaStream_t s);
 int fp32_write(Fp32State& st, const char* name, const void* src, bool from_device, cudaStream_t s);
