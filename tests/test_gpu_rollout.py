@@ -6,8 +6,8 @@ the FP64 form, on conservation figures and on the dambreak front.
   spacing 0.002 m, 6,218 particles, symplectic Euler at dt 1e-5) for 1,000 steps: every
   field bit-identical after the last step, so mass, momentum, energy and the front /
   runout agree up to the summation order of the device reduction (rtol 1e-12).
-* FP32-mixed vs FP64, same 2,000-step dambreak: total mass identical within each form
-  (mass is never updated; drift exactly 0); the change of momentum and of mechanical
+* FP32-mixed vs FP64, same 2,000-step dambreak: total mass constant within each form
+  (mass is never updated; the f64 total moves by summation order only, <= 1e-14); the change of momentum and of mechanical
   energy over the run within 1 % of the FP64 change; the front (largest fluid x) within
   one particle spacing of the FP64 front; the final density field within 1e-3 RMS
   relative error and 1e-2 max relative error (tolerances for a 2,000-step free-surface
@@ -95,8 +95,8 @@ def test_dambreak_2d_2000_steps_fp32_mixed_vs_fp64(native):
     dr = {p: compare.drift(d0[p], s.ps.diagnostics()) for p, s in sims.items()}
     err = compare.field_errors(sims["fp32_mixed"].ps, sims["fp64"].ps, fields=("density", "x"))
     report = f"drift {dr}, errors {err}"
-    for p in sims:
-        assert dr[p]["mass_rel"] == 0.0, report
+    for p in sims:  # mass never changes; the f64 total differs only by summation order
+        assert abs(dr[p]["mass_rel"]) <= 1e-14, report
     m32, m64 = np.array(dr["fp32_mixed"]["momentum"]), np.array(dr["fp64"]["momentum"])
     assert np.linalg.norm(m32 - m64) <= 1e-2 * np.linalg.norm(m64), report
     e32, e64 = dr["fp32_mixed"]["energy"], dr["fp64"]["energy"]

@@ -468,8 +468,7 @@ int fp32_adjoint_step(Fp32State& st, double* ax, double* av, double* ar, double*
     AdjBuffers* B = adj_buffers(st);
     if (!B) return TSG_E_CUDA;
     // forward of the step from the loaded state, keeping its start
-    f32::rebuild(st, s, false);
-    st.cur = 1 - st.cur;
+    f32::rebuild(st, s, false);  // re-sorts into the other buffer and makes it current
     st.built = true;
     st.lists_valid = true;
     ++st.rebuilds;

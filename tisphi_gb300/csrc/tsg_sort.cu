@@ -153,10 +153,15 @@ __device__ __forceinline__ void append(int* list, int* counter, bool pred, int v
     if (pred) list[base + __popc(mask & ((1u << lane) - 1u))] = value;
 }
 
+// vt_src / vt_dst (3 planes each, may be null): v_tmp carried with its particle.  The
+// mu(I) first loop reads the dummy particles' v_tmp of the previous step before the
+// boundary loop rewrites it (eng/solver_sph_muI.py:67-109), and the reference's
+// array-of-structs sort moves it with the particle.
 template <bool SOIL>
 __global__ void k_reorder64(Consts c, const int* __restrict__ perm, Persist64 a, Persist64 b,
                             float4* __restrict__ pos32, int* __restrict__ list_flow,
-                            int* __restrict__ list_bdy, int* __restrict__ list_count) {
+                            int* __restrict__ list_bdy, int* __restrict__ list_count,
+                            const double* __restrict__ vt_src, double* __restrict__ vt_dst) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = k < c.n;
     int mt = 0;
@@ -186,6 +191,8 @@ __global__ void k_reorder64(Consts c, const int* __restrict__ perm, Persist64 a,
         b.obj_id[k] = a.obj_id[s];
         b.is_dynamic[k] = a.is_dynamic[s];
         b.id0[k] = a.id0[s];
+        if (vt_src)
+            for (int d = 0; d < 3; ++d) vt_dst[d * n + k] = vt_src[d * n + s];
         pos32[k] = make_float4((float)(xv[0] - c.vs[0]), (float)(xv[1] - c.vs[1]), (float)(xv[2] - c.vs[2]), 0.f);
     }
     append(list_flow, list_count + 0, live && mt == c.flow_type, k);
@@ -212,10 +219,19 @@ void sort_fp64(const Consts& c, Persist64& cur, Persist64& nxt, Trans64& t, Grid
     scan_exclusive(g.count, g.cell_start, (int)nbins, g.tile_sum, s);
     TSG_LAUNCH(k_scatter, nblk(c.n), TPB, s, c.n, g.cell_of, g.rank, g.cell_start, g.perm);
     TSG_LAUNCH(k_cell_sort, nblk(nbins), TPB, s, nbins, g.cell_start, g.perm);
-    if (c.solver == 1)
-        TSG_LAUNCH(k_reorder64<false>, nblk(c.n), TPB, s, c, g.perm, cur, nxt, t.pos32, g.list_flow, g.list_bdy, g.list_count);
-    else
-        TSG_LAUNCH(k_reorder64<true>, nblk(c.n), TPB, s, c, g.perm, cur, nxt, t.pos32, g.list_flow, g.list_bdy, g.list_count);
+    if (c.solver == 1) {
+        TSG_LAUNCH(k_reorder64<false>, nblk(c.n), TPB, s, c, g.perm, cur, nxt, t.pos32, g.list_flow, g.list_bdy,
+                   g.list_count, nullptr, nullptr);
+    } else {
+        // mu(I) keeps v_tmp across steps: stage it in aux3 (free until advect_pos) and gather
+        const double* src = nullptr;
+        if (c.solver == 2) {
+            cudaMemcpyAsync(t.aux3, t.v_tmp, sizeof(double) * 3 * (size_t)c.n, cudaMemcpyDeviceToDevice, s);
+            src = t.aux3;
+        }
+        TSG_LAUNCH(k_reorder64<true>, nblk(c.n), TPB, s, c, g.perm, cur, nxt, t.pos32, g.list_flow, g.list_bdy,
+                   g.list_count, src, src ? t.v_tmp : nullptr);
+    }
     Persist64 tmp = cur;
     cur = nxt;
     nxt = tmp;
