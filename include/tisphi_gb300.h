@@ -310,6 +310,29 @@ int tsg_snapshot_load(tsg_handle* h, const void* src, void* stream);
 int tsg_adjoint_step(tsg_handle* h, double* adj_x, double* adj_v, double* adj_density, double* adj_v_tmp,
                      double* adj_params, void* stream);
 
+/* Headless visual buffer (replaces the GUI's inputs; no window or graphics API): per
+ * particle the value chosen by color_title (the reference's colour titles: 1 id0,
+ * 2 density, 21 d_density, 3 |v|, 31 v.x, 32 -v.y, 33 v.z, 34 |d_vel|, 35-37 d_vel
+ * components, 4 |x|, 41-43 x components, 44 |x - x0| (FP64 form), 51-57 stress terms,
+ * 61 strain_equ, 62 strain_equ_p, 7 pressure, 8 return-mapping flag, 102 CSPM_L[0][0],
+ * 103 |v_tmp|; assign_value_color, eng/solver_sph_base.py:721-785), its range over the flow
+ * particles with the given / fixed bounds (v_maxmin, eng/particle_system.py:389-398), the
+ * jet colour of the normalised value (set_color, eng/particle_system.py:400-407,
+ * eng/colormap.py:8-50) and the position times w2s_ratio (copy2vis,
+ * eng/particle_system.py:380-386).  pos and color are device float arrays (n, 3) indexed
+ * by particle id (id0); entries the selection leaves out are not written.  range_out (host,
+ * may be NULL) receives (max, min).  TSG_E_ARG for an unknown title, TSG_E_UNSUPPORTED when
+ * the form does not keep the field (x0 in the FP32-mixed form). */
+typedef struct tsg_visual_cfg {
+    int32_t color_title;
+    int32_t color_group;   /* 0 flow, 1 real, 2 real + shown dummies */
+    int32_t show_bdy;
+    int32_t fix_max, fix_min;
+    double w2s_ratio;
+    double given_max, given_min;  /* -1: none */
+} tsg_visual_cfg;
+int tsg_visual(tsg_handle* h, const tsg_visual_cfg* cfg, float* pos, float* color, double* range_out, void* stream);
+
 /* Human-readable text for a status code. */
 const char* tsg_status_string(int status);
 

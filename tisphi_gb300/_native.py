@@ -51,6 +51,12 @@ class tsg_launch_cfg(ctypes.Structure):
                 ("steps_per_graph", ctypes.c_int32)]
 
 
+class tsg_visual_cfg(ctypes.Structure):
+    _fields_ = [("color_title", ctypes.c_int32), ("color_group", ctypes.c_int32), ("show_bdy", ctypes.c_int32),
+                ("fix_max", ctypes.c_int32), ("fix_min", ctypes.c_int32), ("w2s_ratio", ctypes.c_double),
+                ("given_max", ctypes.c_double), ("given_min", ctypes.c_double)]
+
+
 class tsg_view(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("dtype", ctypes.c_int32), ("ndim", ctypes.c_int32),
                 ("shape", ctypes.c_int64 * 3), ("strides", ctypes.c_int64 * 3)]
@@ -74,6 +80,8 @@ SYMBOLS = {
     "tsg_reduce_diag": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "tsg_list_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p]),
     "tsg_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "tsg_visual": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp,
+                                  ctypes.c_void_p]),
     "tsg_set_soil": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]),
     "tsg_snapshot_bytes": (ctypes.c_int64, [ctypes.c_void_p]),
     "tsg_snapshot_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),

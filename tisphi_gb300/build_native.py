@@ -24,6 +24,7 @@ UNITS = {
     "tsg_fp64.cu": ["-fmad=false"],
     "tsg_fp32.cu": [],
     "tsg_adjoint.cu": [],
+    "tsg_visual.cu": ["-fmad=false"],
     "tsg_noalloc.cu": ["-fmad=false"],
 }
 

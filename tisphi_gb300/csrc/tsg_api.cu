@@ -681,6 +681,52 @@ int tsg_last_error(tsg_handle* h, void* stream) {
     return e ? e : v;
 }
 
+int tsg_visual(tsg_handle* h, const tsg_visual_cfg* vc, float* pos, float* color, double* range_out, void* stream) {
+    if (!h || !vc || !pos || !color || !h->uploaded) return TSG_E_ARG;
+    static const int titles[] = {1, 2, 21, 3, 31, 32, 33, 34, 35, 36, 37, 4, 41, 42, 43, 44,
+                                 51, 52, 53, 54, 55, 56, 57, 61, 62, 7, 8, 102, 103};
+    bool known = false;
+    for (int t : titles) known = known || t == vc->color_title;
+    if (!known || vc->color_group < 0 || vc->color_group > 2) return TSG_E_ARG;
+    cudaStream_t s = S(stream);
+    auto view = [&](const char* name, bool needed, const void** out) -> int {
+        *out = nullptr;
+        if (!needed) return 0;
+        tsg_view v;
+        int rc = tsg_field(h, name, &v, stream);
+        if (rc == TSG_E_NAME) return TSG_E_UNSUPPORTED;
+        if (rc) return rc;
+        *out = v.data;
+        return 0;
+    };
+    const int t = vc->color_title;
+    VisFields f{};
+    f.n = h->n;
+    int rc = 0;
+    const void* q = nullptr;
+    if ((rc = view("x", true, &q))) return rc; f.x = static_cast<const double*>(q);
+    if ((rc = view("id0", true, &q))) return rc; f.id0 = static_cast<const int*>(q);
+    if ((rc = view("mat_type", true, &q))) return rc; f.mat_type = static_cast<const int*>(q);
+    if ((rc = view("x0", t == 44, &q))) return rc; f.x0 = static_cast<const double*>(q);
+    if ((rc = view("v", t == 3 || (t >= 31 && t <= 33), &q))) return rc; f.v = static_cast<const double*>(q);
+    if ((rc = view("d_vel", t >= 34 && t <= 37, &q))) return rc; f.d_vel = static_cast<const double*>(q);
+    if ((rc = view("v_tmp", t == 103, &q))) return rc; f.v_tmp = static_cast<const double*>(q);
+    if ((rc = view("density", t == 2, &q))) return rc; f.density = static_cast<const double*>(q);
+    if ((rc = view("d_density", t == 21, &q))) return rc; f.d_density = static_cast<const double*>(q);
+    if ((rc = view("pressure", t == 7, &q))) return rc; f.pressure = static_cast<const double*>(q);
+    if ((rc = view("stress", t >= 51 && t <= 57, &q))) return rc; f.stress = static_cast<const double*>(q);
+    if ((rc = view("strain_equ", t == 61, &q))) return rc; f.strain_equ = static_cast<const double*>(q);
+    if ((rc = view("strain_equ_p", t == 62, &q))) return rc; f.strain_equ_p = static_cast<const double*>(q);
+    if ((rc = view("flag_retmap", t == 8, &q))) return rc; f.flag = static_cast<const int*>(q);
+    if ((rc = view("CSPM_L", t == 102, &q))) return rc; f.CSPM_L = static_cast<const double*>(q);
+    double* scratch = nullptr;
+    if (cudaMalloc(&scratch, sizeof(double) * ((size_t)h->n + 2)) != cudaSuccess) return TSG_E_CUDA;
+    rc = visual_launch(f, *vc, scratch, pos, color, range_out, s);
+    cudaStreamSynchronize(s);
+    cudaFree(scratch);
+    return rc ? rc : check_cuda();
+}
+
 int tsg_set_soil(tsg_handle* h, double friction, double cohesion) {
     if (!h) return TSG_E_ARG;
     Consts& c = h->c;

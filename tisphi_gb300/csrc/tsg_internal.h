@@ -110,6 +110,17 @@ struct Grid {
     int* err;           // device error word
 };
 
+// ---- headless visual buffer (tsg_visual.cu) ----
+// Planar f64 / int views of the fields a colour title may read (null when absent).
+struct VisFields {
+    const double *x, *x0, *v, *d_vel, *v_tmp, *density, *d_density, *pressure, *stress, *strain_equ,
+        *strain_equ_p, *CSPM_L;
+    const int *id0, *mat_type, *flag;
+    int n;
+};
+int visual_launch(const VisFields& f, const tsg_visual_cfg& vc, double* scratch, float* pos, float* col,
+                  double* range_out, cudaStream_t s);
+
 // ---- launchers (tsg_sort.cu) ----
 void sort_fp64(const Consts& c, Persist64& cur, Persist64& nxt, Trans64& t, Grid& g, cudaStream_t s);
 void scan_exclusive(const int* in, int* out, int n, int* tile_sum, cudaStream_t s);

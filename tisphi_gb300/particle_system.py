@@ -182,6 +182,30 @@ class ParticleSystem:
         return {"mass": out[0], "momentum": out[1:4].copy(), "kinetic": out[4], "potential": out[5],
                 "vmax": out[6], "front": out[7]}
 
+    def visual(self, w2s_ratio=None, color_title=None, color_group=None, show_bdy=None, given_max=-1.0,
+               given_min=-1.0, fix_max=False, fix_min=False, pos=None, color=None):
+        """Headless replacement of the GUI inputs (assign_value_color + v_maxmin + set_color +
+        copy2vis, eng/solver_sph_base.py:721-785, eng/particle_system.py:380-407): returns
+        (pos2vis, color, (vmax, vmin)) with pos2vis / color float32 CUDA tensors (n, 3) indexed
+        by id0.  Defaults come from the scene (colorTitle, colorGroup, showBdyPts) and
+        w2s_ratio = 1 / max(domain size) as the reference's GUI sets it (eng/ui_sim.py:33)."""
+        cfg = self.cfg
+        vc = nat.tsg_visual_cfg()
+        vc.color_title = int(cfg.get_cfg("colorTitle") if color_title is None else color_title)
+        vc.color_group = int(cfg.get_cfg("colorGroup") if color_group is None else color_group)
+        vc.show_bdy = int(bool(cfg.get_cfg("showBdyPts") if show_bdy is None else show_bdy))
+        vc.fix_max, vc.fix_min = int(bool(fix_max)), int(bool(fix_min))
+        vc.w2s_ratio = float(1.0 / max(self.domain_size) if w2s_ratio is None else w2s_ratio)
+        vc.given_max, vc.given_min = float(given_max), float(given_min)
+        n = self.particle_max_num
+        pos = torch.zeros((n, 3), dtype=torch.float32, device="cuda") if pos is None else pos
+        color = torch.zeros((n, 3), dtype=torch.float32, device="cuda") if color is None else color
+        rng = np.zeros(2, dtype=np.float64)
+        nat.check(self._lib.tsg_visual(self._h, ctypes.byref(vc), ctypes.c_void_p(pos.data_ptr()),
+                                       ctypes.c_void_p(color.data_ptr()), nat.as_ptr(rng, ctypes.c_double),
+                                       _stream()), "tsg_visual")
+        return pos, color, (float(rng[0]), float(rng[1]))
+
     def list_stats(self):
         """FP32-mixed neighbour-list occupancy: entries of real / dummy particles, overflowed
         particles and list builds since upload (raises for the FP64 form, which keeps no lists)."""
