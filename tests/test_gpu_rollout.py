@@ -12,9 +12,10 @@ the FP64 form, on conservation figures and on the dambreak front.
   one particle spacing of the FP64 front; the final density field within 1e-3 RMS
   relative error and 1e-2 max relative error (tolerances for a 2,000-step free-surface
   flow, where single-step differences of 1e-7 grow through the splash).
-* FP32-mixed vs FP64, granular columns (mu(I), Drucker-Prager; spacing 0.002 m) for 2,000
-  steps: runout (largest soil x) within 0.1 particle spacing of the FP64 runout, and the
-  mean accumulated equivalent strain within 1 % of the FP64 mean.
+* FP32-mixed vs FP64, granular columns (mu(I) with symplectic Euler; Drucker-Prager with
+  leap-frog + XSPH as the reference's sand scene; spacing 0.002 m) for 2,000 steps: runout
+  (largest soil x) within 0.1 particle spacing of the FP64 runout, and the mean
+  accumulated equivalent strain within 1 % of the FP64 mean.
 """
 import numpy as np
 import pytest
@@ -111,7 +112,12 @@ def test_column_2000_steps_fp32_mixed_vs_fp64(native, method):
 
     from tisphi_gb300 import compare
     from tisphi_gb300.simulation import Simulation
-    cfg = cfg_of(small_column(method, spacing=0.002))
+    # Drucker-Prager with the reference's own sand-scene settings (leap-frog + XSPH,
+    # data/scenes/test2_cc_sand.json): with symplectic Euler and no XSPH the reference's DP
+    # formulation is unstable at this resolution (the FP64 form, bit-identical to the
+    # oracle, gains 7x its initial mechanical energy within 1,400 steps)
+    extra = {} if method == 2 else {"integration": 2, "xsph": True}
+    cfg = cfg_of(small_column(method, spacing=0.002, **extra))
     sims = {p: Simulation(cfg, precision=p) for p in ("fp32_mixed", "fp64")}
     d0 = {p: s.ps.diagnostics() for p, s in sims.items()}
     for s in sims.values():

@@ -36,13 +36,14 @@ namespace {
 
 // Step-start copies (sorted order) and the adjoint work arrays.
 struct Start {
-    float4 *hi, *lo, *vel, *vt;
+    float4 *hi, *lo, *vel, *vlo, *vt;
     float* drho;
 };
 struct A32 {
     float2 *x, *v, *dv, *vn, *b1;
     float *r, *mv, *rt, *dr, *b2, *bs, *dds;
     float4 *s, *b3, *vg;  // full 2 x 2 matrices: (xx, xy, yx, yy)
+    double2* gp;          // per-particle (d/d mu, d/d cohesion), reduced in a fixed order
 };
 
 // dG/dr of the gradient factor G (grad W = G d).
@@ -274,24 +275,34 @@ __global__ void k_adj_bdy_soil(K32 k, P32 p, T32 t, Start S, A32 A) {
     A.r[j] += ar;
 }
 
-__device__ __forceinline__ float2 vt_start(const Start& S, int j) {
-    return soil(S.lo[j].w) ? f2(S.vel[j].x, S.vel[j].y) : f2(S.vt[j].x, S.vt[j].y);
+// v~ at the step start as hi + lo: the soil velocity (compensated), the dummies' previous
+// extrapolated velocity (single f32).
+struct Vc {
+    float hx, hy, lx, ly;
+};
+__device__ __forceinline__ Vc vt_start(const Start& S, int j) {
+    if (soil(S.lo[j].w)) return {S.vel[j].x, S.vel[j].y, S.vlo[j].x, S.vlo[j].y};
+    return {S.vt[j].x, S.vt[j].y, 0.f, 0.f};
+}
+__device__ __forceinline__ float2 vdiff(const Vc& a, const Vc& b) {  // a - b
+    return f2(dv_comp(a.hx, a.lx, b.hx, b.lx), dv_comp(a.hy, a.ly, b.hy, b.ly));
 }
 
 // ---- K5: mu(I) stress and continuity reversed at each soil particle, its own side of
 // the velocity-gradient sums; parameter adjoints ----
-__global__ void k_adj_stress(K32 k, P32 p, T32 t, Start S, A32 A, double* __restrict__ pbar) {
+__global__ void k_adj_stress(K32 k, P32 p, T32 t, Start S, A32 A) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
     double gmu = 0.0, gcoh = 0.0;
-    if (i < k.n && soil(S.lo[i].w)) {
-        const float2 vi = vt_start(S, i);
+    if (soil(S.lo[i].w)) {
+        const Vc vi = vt_start(S, i);
         float vxx = 0.f, vxy = 0.f, vyx = 0.f, vyy = 0.f;
         for_list(k, t, i, [&](int j) {
             Pair P;
             if (!pair(k, S, i, j, P)) return;
             const float mvj = S.hi[j].w;
-            const float2 vj = vt_start(S, j);
-            const float ux = mvj * (vj.x - vi.x), uy = mvj * (vj.y - vi.y);
+            const float2 u = vdiff(vt_start(S, j), vi);
+            const float ux = mvj * u.x, uy = mvj * u.y;
             const float gx = P.G * P.dx, gy = P.G * P.dy;
             vxx += ux * gx; vxy += ux * gy; vyx += uy * gx; vyy += uy * gy;
         });
@@ -323,8 +334,8 @@ __global__ void k_adj_stress(K32 k, P32 p, T32 t, Start S, A32 A, double* __rest
             Pair P;
             if (!pair(k, S, i, j, P)) return;
             const float mvj = S.hi[j].w;
-            const float2 vj = vt_start(S, j);
-            const float ux = vj.x - vi.x, uy = vj.y - vi.y;
+            const float2 u = vdiff(vt_start(S, j), vi);
+            const float ux = u.x, uy = u.y;
             const float gx = P.G * P.dx, gy = P.G * P.dy;
             av.x -= mvj * (gxx * gx + gxy * gy - ddb * gx);
             av.y -= mvj * (gxy * gx + gyy * gy - ddb * gy);
@@ -338,13 +349,31 @@ __global__ void k_adj_stress(K32 k, P32 p, T32 t, Start S, A32 A, double* __rest
         A.x[i] = f2(A.x[i].x + ax.x, A.x[i].y + ax.y);
         A.r[i] += ar;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        gmu += __shfl_down_sync(0xffffffffu, gmu, o);
-        gcoh += __shfl_down_sync(0xffffffffu, gcoh, o);
+    A.gp[i] = make_double2(gmu, gcoh);
+}
+
+// Parameter adjoints summed in a fixed order (one block, strided partials, tree), so that
+// repeated reversals of the same step give the same bits.
+__global__ void k_adj_params(int n, const double2* __restrict__ gp, double* __restrict__ pbar) {
+    __shared__ double smu[256], sco[256];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        a += gp[i].x;
+        b += gp[i].y;
     }
-    if ((threadIdx.x & 31) == 0 && (gmu != 0.0 || gcoh != 0.0)) {
-        atomicAdd(&pbar[0], gmu);
-        atomicAdd(&pbar[1], gcoh);
+    smu[threadIdx.x] = a;
+    sco[threadIdx.x] = b;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            smu[threadIdx.x] += smu[threadIdx.x + w];
+            sco[threadIdx.x] += sco[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        pbar[0] += smu[0];
+        pbar[1] += sco[0];
     }
 }
 
@@ -354,7 +383,7 @@ __global__ void k_adj_vgrad(K32 k, P32 p, T32 t, Start S, A32 A) {
     if (kk >= k.n) return;
     const bool ks = soil(S.lo[kk].w);
     const float mvk = S.hi[kk].w;
-    const float2 vk = vt_start(S, kk);
+    const Vc vk = vt_start(S, kk);
     float2 av = f2(0.f, 0.f), ax = f2(0.f, 0.f);
     float amv = 0.f;
     for_list(k, t, kk, [&](int i) {
@@ -363,8 +392,8 @@ __global__ void k_adj_vgrad(K32 k, P32 p, T32 t, Start S, A32 A) {
         if (!pair(k, S, kk, i, P)) return;
         const float4 g4 = A.vg[i];
         const float ddb = A.dds[i];
-        const float2 vi = vt_start(S, i);
-        const float ux = vk.x - vi.x, uy = vk.y - vi.y;       // u_ik = v~_k - v~_i
+        const float2 u = vdiff(vk, vt_start(S, i));           // u_ik = v~_k - v~_i
+        const float ux = u.x, uy = u.y;
         const float dx = -P.dx, dy = -P.dy;                    // d_ik = x_i - x_k
         const float gx = P.G * dx, gy = P.G * dy;
         const float wgx = g4.x * gx + g4.y * gy - ddb * gx, wgy = g4.z * gx + g4.w * gy - ddb * gy;
@@ -413,6 +442,7 @@ __global__ void k_copy_start(int n, P32 p, const float4* __restrict__ vt, Start 
     S.hi[i] = p.hi[i];
     S.lo[i] = p.lo[i];
     S.vel[i] = p.vel[i];
+    S.vlo[i] = p.vlo[i];
     S.drho[i] = p.drho[i];
     S.vt[i] = vt[i];
 }
@@ -437,13 +467,15 @@ AdjBuffers* adj_buffers(Fp32State& st) {
     Start& S = b->S;
     A32& A = b->A;
     S.hi = grab<float4>(st, n); S.lo = grab<float4>(st, n); S.vel = grab<float4>(st, n); S.vt = grab<float4>(st, n);
+    S.vlo = grab<float4>(st, n);
+    A.gp = grab<double2>(st, n);
     S.drho = grab<float>(st, n);
     A.x = grab<float2>(st, n); A.v = grab<float2>(st, n); A.dv = grab<float2>(st, n); A.vn = grab<float2>(st, n);
     A.b1 = grab<float2>(st, n);
     A.r = grab<float>(st, n); A.mv = grab<float>(st, n); A.rt = grab<float>(st, n); A.dr = grab<float>(st, n);
     A.b2 = grab<float>(st, n); A.bs = grab<float>(st, n); A.dds = grab<float>(st, n);
     A.s = grab<float4>(st, n); A.b3 = grab<float4>(st, n); A.vg = grab<float4>(st, n);
-    if (!S.hi || !S.lo || !S.vel || !S.vt || !S.drho || !A.x || !A.v || !A.dv || !A.vn || !A.b1 || !A.r || !A.mv ||
+    if (!S.hi || !S.lo || !S.vel || !S.vt || !S.vlo || !A.gp || !S.drho || !A.x || !A.v || !A.dv || !A.vn || !A.b1 || !A.r || !A.mv ||
         !A.rt || !A.dr || !A.b2 || !A.bs || !A.dds || !A.s || !A.b3 || !A.vg) {
         delete b;
         return nullptr;
@@ -485,7 +517,8 @@ int fp32_adjoint_step(Fp32State& st, double* ax, double* av, double* ar, double*
     TSG_LAUNCH(k_adj_mom, nb, TPB, s, k, p, st.T, B->S, B->A);
     TSG_LAUNCH(k_adj_bdy, nb, TPB, s, k, p, st.T, B->S, B->A);
     TSG_LAUNCH(k_adj_bdy_soil, nb, TPB, s, k, p, st.T, B->S, B->A);
-    TSG_LAUNCH(k_adj_stress, nb, TPB, s, k, p, st.T, B->S, B->A, pbar);
+    TSG_LAUNCH(k_adj_stress, nb, TPB, s, k, p, st.T, B->S, B->A);
+    TSG_LAUNCH(k_adj_params, 1, 256, s, st.n, B->A.gp, pbar);
     TSG_LAUNCH(k_adj_vgrad, nb, TPB, s, k, p, st.T, B->S, B->A);
     TSG_LAUNCH(k_adj_out, nb, TPB, s, k, p, B->S, B->A, ax, av, ar, avt);
     return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;

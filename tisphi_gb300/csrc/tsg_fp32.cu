@@ -103,6 +103,7 @@ __global__ void k_reorder32(K32 k, int count_n, int base, const int* __restrict_
         b.eeqp[dst] = a.eeqp[src];
         b.flag[dst] = a.flag[src];
     }
+    if (a.vlo) b.vlo[dst] = a.vlo[src];
     PF[dst] = make_float4(pfv[0], pfv[1], pfv[2], l.w);
 }
 
@@ -350,6 +351,7 @@ __global__ void k_init_tmp32(K32 k, P32 p, T32 t) {
         const size_t n = k.n;
         for (int q = 0; q < 6; ++q) t.sigt[q * n + i] = p.sig[q * n + i];
     }
+    if (ti > 0 && t.vtlo) t.vtlo[i] = p.vlo[i];
 }
 
 // Tait EOS from the density deviation e = (rho_tmp - rho0) / rho0:
@@ -501,7 +503,7 @@ __global__ void k_mui_stress32(K32 k, P32 p, T32 t, const float4* __restrict__ P
                                const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
       if (tf_type(p.lo[i].w) == MAT_SOIL) {
-        const float4 vti = t.vt[i];
+        const float4 vti = t.vt[i], vli = t.vtlo[i];
         float L[9];
         if (CORR)
             for (int q = 0; q < 9; ++q) L[q] = t.L[(size_t)q * k.n + i];
@@ -511,7 +513,7 @@ __global__ void k_mui_stress32(K32 k, P32 p, T32 t, const float4* __restrict__ P
                           [&](int j, const float* d, float r2, int sidx) {
             float kc[3];
             grad_c<DIM, CORR>(L, w_grad(k, fast_sqrt(r2)), d, kc);
-            vgrad_add<DIM>(p.hi[j].w, vti, t.vt[j], kc, vg, dd);
+            vgrad_add<DIM>(p.hi[j].w, vti, vli, t.vt[j], t.vtlo[j], kc, vg, dd);
             if ((sidx & 7) == 7) dd.flush();
         });
         const size_t n = k.n;
@@ -579,7 +581,7 @@ __global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
       if (tf_type(p.lo[i].w) == MAT_SOIL) {
         const size_t n = k.n;
-        const float4 vti = t.vt[i];
+        const float4 vti = t.vt[i], vli = t.vtlo[i];
         float L[9];
         if (CORR)
             for (int q = 0; q < 9; ++q) L[q] = t.L[(size_t)q * n + i];
@@ -616,7 +618,7 @@ __global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
                 dv[0].add(coef * (mxx * kc[0] + mxy * kc[1]));
                 dv[1].add(coef * (mxy * kc[0] + myy * kc[1]));
             }
-            if (DP) vgrad_add<DIM>(mVj, vti, t.vt[j], kc, vg, dd);
+            if (DP) vgrad_add<DIM>(mVj, vti, vli, t.vt[j], t.vtlo[j], kc, vg, dd);
             if (rep_on && tf_type(p.lo[j].w) == MAT_REP) {  // eng/solver_sph_base.py:675-689
                 const float chi = (r > 0.f && r < k.diam) ? 1.f - r / k.diam : 0.f;
                 const float gm = r / k.h075;
@@ -764,7 +766,15 @@ __global__ void k_advect_half32(K32 k, P32 p, T32 t) {
     p.hi[i].w = p.mass[i] / (k.rho0 + drt);
     const float4 dv = t.dv[i];
     float4 vt = t.vt[i];
-    vt.x += k.hdt * dv.x; vt.y += k.hdt * dv.y; vt.z += k.hdt * dv.z;
+    if (t.vtlo) {
+        float4 vl = t.vtlo[i];
+        two_sum_add(vt.x, vl.x, k.hdt * dv.x);
+        two_sum_add(vt.y, vl.y, k.hdt * dv.y);
+        two_sum_add(vt.z, vl.z, k.hdt * dv.z);
+        t.vtlo[i] = vl;
+    } else {
+        vt.x += k.hdt * dv.x; vt.y += k.hdt * dv.y; vt.z += k.hdt * dv.z;
+    }
     t.vt[i] = vt;
 }
 
@@ -782,7 +792,15 @@ __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
     p.hi[i].w = p.mass[i] / (k.rho0 + dr);
     const float4 dv = t.dv[i];
     float4 v = p.vel[i];
-    v.x += k.dt * dv.x; v.y += k.dt * dv.y; v.z += k.dt * dv.z;
+    if (p.vlo) {
+        float4 vl = p.vlo[i];
+        two_sum_add(v.x, vl.x, k.dt * dv.x);
+        two_sum_add(v.y, vl.y, k.dt * dv.y);
+        two_sum_add(v.z, vl.z, k.dt * dv.z);
+        p.vlo[i] = vl;
+    } else {
+        v.x += k.dt * dv.x; v.y += k.dt * dv.y; v.z += k.dt * dv.z;
+    }
     p.vel[i] = v;
     if (!isfinite(dr)) atomicOr(err, TSG_ERR_NONFINITE);
 }
@@ -815,7 +833,11 @@ __global__ void k_advect_pos32(K32 k, P32 p, T32 t, int* err) {
     if (i >= k.nd) return;
     const float w = p.lo[i].w;
     if (tf_type(w) <= 0) return;
-    const float4 v = p.vel[i];
+    float4 v = p.vel[i];
+    if (p.vlo) {
+        const float4 vl = p.vlo[i];
+        v.x += vl.x; v.y += vl.y; v.z += vl.z;
+    }
     float4 l = p.lo[i];
     if (k.xsph && tf_dyn(w)) {
         const float4 s = t.xs[i];
@@ -887,12 +909,22 @@ __global__ void k_export(K32 k, P32 p, T32 t, int what, double* out) {
         out[2 * n + i] = k.vs[2] + ((double)h.z + (double)l.z);
         break;
     }
-    case 1: { float4 v = p.vel[i]; out[i] = v.x; out[n + i] = v.y; out[2 * n + i] = v.z; break; }
+    case 1: {
+        const float4 v = p.vel[i];
+        const float4 vl = p.vlo ? p.vlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        out[i] = (double)v.x + vl.x; out[n + i] = (double)v.y + vl.y; out[2 * n + i] = (double)v.z + vl.z;
+        break;
+    }
     case 2: out[i] = tf_type(p.lo[i].w) > 0 ? (double)k.rho0 + (double)p.drho[i] : 0.0; break;  // density
     case 3: out[i] = p.vel[i].w; break;                       // pressure
     case 4: out[i] = p.hi[i].w; break;                        // m_V
     case 5: out[i] = p.mass[i]; break;                        // mass
-    case 6: { float4 v = t.vt[i]; out[i] = v.x; out[n + i] = v.y; out[2 * n + i] = v.z; break; }  // v_tmp
+    case 6: {  // v_tmp
+        const float4 v = t.vt[i];
+        const float4 vl = t.vtlo ? t.vtlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        out[i] = (double)v.x + vl.x; out[n + i] = (double)v.y + vl.y; out[2 * n + i] = (double)v.z + vl.z;
+        break;
+    }
     case 7: out[i] = (double)k.rho0 + (double)t.drt[i]; break;  // density_tmp
     case 8: out[i] = t.dd[i]; break;
     case 9: { float4 v = t.dv[i]; out[i] = v.x; out[n + i] = v.y; out[2 * n + i] = v.z; break; }
@@ -940,7 +972,14 @@ __global__ void k_import(K32 k, P32 p, int what, const double* in) {
         p.lo[i] = l;
         break;
     }
-    case 1: { float4 v = p.vel[i]; v.x = (float)in[i]; v.y = (float)in[n + i]; v.z = (float)in[2 * n + i]; p.vel[i] = v; break; }
+    case 1: {
+        float4 v = p.vel[i];
+        const double a = in[i], b = in[n + i], c = in[2 * n + i];
+        v.x = (float)a; v.y = (float)b; v.z = (float)c;
+        p.vel[i] = v;
+        if (p.vlo) p.vlo[i] = make_float4((float)(a - v.x), (float)(b - v.y), (float)(c - v.z), 0.f);
+        break;
+    }
     case 2: if (tf_type(p.lo[i].w) > 0) p.drho[i] = (float)(in[i] - (double)k.rho0); break;
     case 3: p.vel[i].w = (float)in[i]; break;
     default: break;
@@ -1005,7 +1044,9 @@ __global__ void k_load32(K32 k, const double* __restrict__ x, const double* __re
     const int word = 0x40000000 | (mt[s] & 0xffff) | ((dyn[s] & 1) << 16) | (sc << 17);
     p.hi[i] = make_float4(hv[0], hv[1], hv[2], (float)mV[s]);
     p.lo[i] = make_float4(lv[0], lv[1], lv[2], __int_as_float(word));
-    p.vel[i] = make_float4((float)v[3 * (size_t)s], (float)v[3 * (size_t)s + 1], (float)v[3 * (size_t)s + 2], (float)pres[s]);
+    const double v0 = v[3 * (size_t)s], v1 = v[3 * (size_t)s + 1], v2 = v[3 * (size_t)s + 2];
+    p.vel[i] = make_float4((float)v0, (float)v1, (float)v2, (float)pres[s]);
+    if (p.vlo) p.vlo[i] = make_float4((float)(v0 - (float)v0), (float)(v1 - (float)v1), (float)(v2 - (float)v2), 0.f);
     p.drho[i] = mt[s] > 0 ? (float)(dens[s] - (double)k.rho0) : 0.f;
     p.mass[i] = (float)mass[s];
     p.ids[i] = make_int4(s, mid[s], oid[s], dyn[s]);
@@ -1323,6 +1364,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
         if (soil) {
             st->P[q].sig = dal<float>(*st, 6 * (size_t)n); st->P[q].eeq = dal<float>(*st, n);
             st->P[q].eeqp = dal<float>(*st, n); st->P[q].flag = dal<int>(*st, n);
+            st->P[q].vlo = dal<float4>(*st, n);
         }
     }
     T32& t = st->T;
@@ -1332,6 +1374,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     t.cnt = dal<int>(*st, n);
     t.nbr = dal<int>(*st, (size_t)k.maxn * n);
     if (soil) {
+        t.vtlo = dal<float4>(*st, n);
         t.sigt = dal<float>(*st, 6 * (size_t)n); t.dee = dal<float>(*st, n);
         if (c.solver == 3) { t.dsig = dal<float>(*st, 6 * (size_t)n); t.deep = dal<float>(*st, n); }
     }
@@ -1423,6 +1466,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
             cudaMemcpyAsync(dst.eeq + off, src.eeq + off, sizeof(float) * ns, cudaMemcpyDeviceToDevice, s);
             cudaMemcpyAsync(dst.eeqp + off, src.eeqp + off, sizeof(float) * ns, cudaMemcpyDeviceToDevice, s);
             cudaMemcpyAsync(dst.flag + off, src.flag + off, sizeof(int) * ns, cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(dst.vlo + off, src.vlo + off, sizeof(float4) * ns, cudaMemcpyDeviceToDevice, s);
         }
     } else {
         cudaMemsetAsync(st->sstart, 0, sizeof(int) * (k.G + 2), s);
@@ -1507,6 +1551,7 @@ __global__ void k_copy_back32(int nd, P32 b, P32 a, size_t n) {
         a.eeqp[i] = b.eeqp[i];
         a.flag[i] = b.flag[i];
     }
+    if (a.vlo) a.vlo[i] = b.vlo[i];
 }
 
 }  // namespace
@@ -1884,6 +1929,7 @@ std::vector<std::pair<void*, size_t>> snap_items(Fp32State& st) {
         v.push_back({p.eeqp, sizeof(float) * n});
         v.push_back({p.flag, sizeof(int) * n});
     }
+    if (p.vlo) v.push_back({p.vlo, sizeof(float4) * n});
     return v;
 }
 

@@ -250,6 +250,7 @@ struct P32 {
     float* eeq;     // equivalent strain
     float* eeqp;    // equivalent plastic strain (Drucker-Prager)
     int* flag;      // return-mapping case (Drucker-Prager)
+    float4* vlo;    // velocity low part: v = vel.xyz + vlo.xyz (compensated time integration)
 };
 
 // Symmetric 3x3 tensors are stored as six planes: xx, yy, zz, xy, xz, yz.
@@ -272,7 +273,24 @@ struct T32 {
     float* dsig;    // d_stress, 6 planes (Drucker-Prager)
     float* dee;     // d_strain_equ
     float* deep;    // d_strain_equ_p (Drucker-Prager)
+    float4* vtlo;   // v_tmp low part (zero for dummies)
 };
+
+// Compensated velocities of the granular solvers.  The strain rate of mu(I) is regularised
+// only by 1e-8 1/s, so in regions of near-rigid motion (a free-falling surface layer) the
+// f32 rounding noise of stored velocities (~1e-6 1/s of spurious strain rate) would set the
+// stress direction and its sensitivity to cohesion; keeping v as an unevaluated sum
+// hi + lo (two f32) makes velocity differences exact to ~1e-14 relative.
+__device__ __forceinline__ void two_sum_add(float& hi, float& lo, float a) {
+    const float s = hi + a;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (a - bb);
+    const float l = lo + e;
+    hi = s + l;
+    lo = l - (hi - s);
+}
+// (vj - vi) of two compensated velocities, component-wise.
+__device__ __forceinline__ float dv_comp(float hj, float lj, float hi_, float li) { return (hj - hi_) + (lj - li); }
 
 // ---------------------------------------------------------------- granular solvers
 // Drucker-Prager invariants and stress adaptation (eng/solver_sph_dp.py:42-109) on the
@@ -330,9 +348,10 @@ __device__ __forceinline__ void grad_c(const float* L, float gf, const float* d,
 
 // Velocity gradient sum_j m_Vj (v_j - v_i) (x) kc and continuity sum_j m_Vj (v_i - v_j) . kc.
 template <int DIM>
-__device__ __forceinline__ void vgrad_add(float mVj, const float4& vti, const float4& vtj, const float* kc, float* vg,
-                                          CSum& dd) {
-    const float u[3] = {mVj * (vtj.x - vti.x), mVj * (vtj.y - vti.y), DIM == 3 ? mVj * (vtj.z - vti.z) : 0.f};
+__device__ __forceinline__ void vgrad_add(float mVj, const float4& vti, const float4& vli, const float4& vtj,
+                                          const float4& vlj, const float* kc, float* vg, CSum& dd) {
+    const float u[3] = {mVj * dv_comp(vtj.x, vlj.x, vti.x, vli.x), mVj * dv_comp(vtj.y, vlj.y, vti.y, vli.y),
+                        DIM == 3 ? mVj * dv_comp(vtj.z, vlj.z, vti.z, vli.z) : 0.f};
 #pragma unroll
     for (int a = 0; a < DIM; ++a)
 #pragma unroll
