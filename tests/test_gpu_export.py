@@ -89,9 +89,11 @@ def test_visual_buffer(native, precision, scene, title, group, show):
     flow = (mt == 1) | (mt == 2)
     assert vmax == val[flow].max() and vmin == val[flow].min()
     real = mt > 0
-    shown = real | (show & ((mt == -1) | (mt == -2)))
+    bdy = (mt == -1) | (mt == -2)
+    shown = real | (bdy if show else np.zeros_like(real))
     np.testing.assert_array_equal(pos[ids[shown]], (x[shown] * w2s).astype(np.float32))
-    pick = {0: flow, 1: real, 2: real | (show & (mt == -1))}[group]
+    assert np.all(pos[ids[~shown]] == 0)
+    pick = {0: flow, 1: real, 2: real | ((mt == -1) if show else np.zeros_like(real))}[group]
     ref = _jet((val[pick] - vmin) * (1.0 / (vmax - vmin))).astype(np.float32)
     np.testing.assert_allclose(col[ids[pick]], ref, rtol=0, atol=1.2e-7)
     assert np.all(col[ids[~pick]] == 0)

@@ -71,7 +71,7 @@ def step(x, v, rho, vt_prev, mu, coh, C):
     sJ = torch.sqrt(torch.where(pos, J, torch.ones_like(J))) * pos
     dbdot = sJ + 1e-8
     sc = (coh + p * mu) / dbdot
-    I2 = torch.eye(2, dtype=torch.float64)
+    I2 = torch.eye(2, dtype=x.dtype)
     sig = sc[:, None, None] * er - p[:, None, None] * I2
     # boundary extrapolation (dummies)
     B1 = Wb @ vt
