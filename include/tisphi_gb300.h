@@ -242,7 +242,7 @@ int tsg_sort_noalloc(const tsg_config* cfg, const double* x, int64_t n, int32_t*
 
 /* Launch configuration of the FP32-mixed form.  No reference counterpart (Taichi picks
  * its own launch shapes): threads_per_block of the neighbour-traversal kernels (64, 128,
- * 256, 512); cells_per_cta of the neighbour-list build, one warp per cell (2, 4, 8; 0 = one
+ * 256); cells_per_cta of the neighbour-list build, one warp per cell (2, 4, 8; 0 = one
  * thread per particle); steps_per_graph, how many steps one captured CUDA graph replays
  * (1..64).  tsg_step runs FP32-mixed steps as graph replays (each step re-sorts inside the
  * graph only when the device-side displacement check asks for it); while tsg_profile is

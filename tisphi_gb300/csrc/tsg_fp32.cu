@@ -422,7 +422,7 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
 
 // WCSPH continuity + momentum (eng/solver_sph_wc.py:108-126).
 template <int DIM, bool FB, bool CORR>
-__global__ void k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
+__global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                           const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
       const float wi = p.lo[i].w;
@@ -1901,7 +1901,7 @@ void fp32_get_launch(const Fp32State& st, int* tpb, int* cpc, int* spg) {
 }
 
 int fp32_set_launch(Fp32State& st, int tpb, int cpc, int spg) {
-    if (tpb != 64 && tpb != 128 && tpb != 256 && tpb != 512) return TSG_E_ARG;
+    if (tpb != 64 && tpb != 128 && tpb != 256) return TSG_E_ARG;  // kernels are bounded for 256
     if (cpc != 0 && cpc != 2 && cpc != 4 && cpc != 8) return TSG_E_ARG;
     if (spg < 1 || spg > 64) return TSG_E_ARG;
     st.tpb = tpb;
