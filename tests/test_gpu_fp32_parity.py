@@ -123,7 +123,7 @@ def test_one_step_rates_close(oracle_lib, native, scene, corr):
 
 
 @pytest.mark.parametrize("scene,ti,skin", [("2d", 2, 0.1), ("2d", 1, 0.1), ("3d", 2, 0.1), ("2d", 2, 0.0),
-                                           ("3d", 2, 0.0), ("2d", 2, 0.002)])
+                                           ("3d", 2, 0.0), ("2d", 2, 0.002), ("2d", 4, 0.1), ("3d", 4, 0.1)])
 def test_steps_density_position(oracle_lib, native, scene, ti, skin):
     """Neighbour-list skin 0.1 R: lists reused across steps; 0: rebuilt every step; 0.002 R:
     rebuilt whenever a particle moves 0.0009 R (several rebuilds within the run)."""
@@ -169,7 +169,7 @@ def test_soil_one_step_rates_close(oracle_lib, native, method):
     assert all(e < 1e-4 for e in errs.values()), f"normwise errors {errs}"
 
 
-@pytest.mark.parametrize("method,ti", [(2, 1), (3, 1), (3, 2)])
+@pytest.mark.parametrize("method,ti", [(2, 1), (3, 1), (3, 2), (2, 4), (3, 4)])
 def test_soil_steps_close(oracle_lib, native, method, ti):
     sim, orc = _pair(small_column(method, integration=ti), oracle_lib)
     _advance(sim, orc, oracle_lib, 20)

@@ -778,6 +778,83 @@ __global__ void k_advect_half32(K32 k, P32 p, T32 t) {
     t.vt[i] = vt;
 }
 
+// ---- RK4 (eng/solver_sph_base.py:134-180): accumulate m * rates over the four one_steps;
+// the intermediate states use dt / 2 from the step-start values (the reference's stages)
+__global__ void k_rk_init32(K32 k, P32 p, T32 t) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd) return;
+    const int ti = tf_type(p.lo[i].w);
+    if (ti <= 0) return;
+    t.ddrk[i] = 0.f;
+    t.dvrk[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (ti == MAT_SOIL && t.dsigrk)
+        for (int q = 0; q < 6; ++q) t.dsigrk[(size_t)q * k.n + i] = 0.f;
+}
+
+__global__ void k_rk_update32(K32 k, P32 p, T32 t, float m) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd) return;
+    const int ti = tf_type(p.lo[i].w);
+    if (ti <= 0) return;
+    t.ddrk[i] += t.dd[i] * m;
+    const float4 dv = t.dv[i];
+    float4 a = t.dvrk[i];
+    a.x += dv.x * m; a.y += dv.y * m; a.z += dv.z * m;
+    t.dvrk[i] = a;
+    if (ti == MAT_SOIL && t.dsigrk)
+        for (int q = 0; q < 6; ++q) t.dsigrk[(size_t)q * k.n + i] += m * t.dsig[(size_t)q * k.n + i];
+}
+
+__global__ void k_rk_stage32(K32 k, P32 p, T32 t) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd) return;
+    const int ti = tf_type(p.lo[i].w);
+    if (ti <= 0) return;
+    const float drt = k.hdt * t.dd[i] + p.drho[i];
+    t.drt[i] = drt;
+    p.hi[i].w = p.mass[i] / (k.rho0 + drt);
+    const float4 dv = t.dv[i];
+    float4 vt = p.vel[i];
+    if (t.vtlo) {
+        float4 vl = p.vlo[i];
+        two_sum_add(vt.x, vl.x, k.hdt * dv.x);
+        two_sum_add(vt.y, vl.y, k.hdt * dv.y);
+        two_sum_add(vt.z, vl.z, k.hdt * dv.z);
+        t.vtlo[i] = vl;
+    } else {
+        vt.x = k.hdt * dv.x + vt.x; vt.y = k.hdt * dv.y + vt.y; vt.z = k.hdt * dv.z + vt.z;
+    }
+    t.vt[i] = make_float4(vt.x, vt.y, vt.z, t.vt[i].w);
+    if (ti == MAT_SOIL && k.solver == 3)
+        for (int q = 0; q < 6; ++q)
+            t.sigt[(size_t)q * k.n + i] = k.hdt * t.dsig[(size_t)q * k.n + i] + p.sig[(size_t)q * k.n + i];
+}
+
+__global__ void k_rk_final32(K32 k, P32 p, T32 t, int* err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd) return;
+    const int ti = tf_type(p.lo[i].w);
+    if (ti <= 0) return;
+    const float dr = p.drho[i] + k.dt6 * t.ddrk[i];
+    p.drho[i] = dr;
+    p.hi[i].w = p.mass[i] / (k.rho0 + dr);
+    const float4 a = t.dvrk[i];
+    float4 v = p.vel[i];
+    if (p.vlo) {
+        float4 vl = p.vlo[i];
+        two_sum_add(v.x, vl.x, k.dt6 * a.x);
+        two_sum_add(v.y, vl.y, k.dt6 * a.y);
+        two_sum_add(v.z, vl.z, k.dt6 * a.z);
+        p.vlo[i] = vl;
+    } else {
+        v.x += k.dt6 * a.x; v.y += k.dt6 * a.y; v.z += k.dt6 * a.z;
+    }
+    p.vel[i] = v;
+    if (ti == MAT_SOIL && k.solver == 3)
+        for (int q = 0; q < 6; ++q) p.sig[(size_t)q * k.n + i] += k.dt6 * t.dsigrk[(size_t)q * k.n + i];
+    if (!isfinite(dr)) atomicOr(err, TSG_ERR_NONFINITE);
+}
+
 __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
@@ -1292,7 +1369,7 @@ __global__ void k_offset(int* a, long long m, int off) {
 int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp, bool from_device,
                 Fp32State** out, cudaStream_t s, const Fp32Scenes* scenes) {
     *out = nullptr;
-    if (c.ti == 4) return TSG_E_UNSUPPORTED;  // SE / LF in this form
+
     Fp32State* st = new Fp32State();
     st->c = c;
     const int n = c.n;
@@ -1317,7 +1394,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     k.R2lo = (float)(c.R * c.R * (1.0 - 1.0 / 1024.0));
     k.pf_lim = (float)(500.0 * c.R);
     k.visc_fac = (float)c.visc_fac; k.eps_h2 = (float)c.eps_h2; k.rho0 = (float)c.rho0; k.B = (float)c.B;
-    k.gamma = (float)c.gamma; k.dt = (float)c.dt; k.hdt = (float)c.hdt;
+    k.gamma = (float)c.gamma; k.dt = (float)c.dt; k.hdt = (float)c.hdt; k.dt6 = (float)c.dt6;
     k.rep_fac = (float)c.rep_fac; k.diam = (float)c.diam; k.h075 = (float)c.h075; k.r_eps = (float)c.r_eps;
     k.mu = (float)c.mu; k.c2 = (float)c.vsound2; k.coh = (float)c.coh; k.alpha = (float)c.alpha;
     k.k_c = (float)c.k_c; k.kc_over_alpha = (float)c.kc_over_alpha; k.Gm = (float)c.Gm; k.Km = (float)c.Km;
@@ -1373,6 +1450,11 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     t.L = c.corr == 1 ? dal<float>(*st, 9 * (size_t)n) : nullptr;
     t.cnt = dal<int>(*st, n);
     t.nbr = dal<int>(*st, (size_t)k.maxn * n);
+    if (c.ti == 4) {
+        t.ddrk = dal<float>(*st, n);
+        t.dvrk = dal<float4>(*st, n);
+        if (c.solver == 3) t.dsigrk = dal<float>(*st, 6 * (size_t)n);
+    }
     if (soil) {
         t.vtlo = dal<float4>(*st, n);
         t.sigt = dal<float>(*st, 6 * (size_t)n); t.dee = dal<float>(*st, n);
@@ -1751,11 +1833,17 @@ void fp32_advect(Fp32State& st, int which, cudaStream_t s) {
         break;
     }
     case TSG_ENFORCE_BOUNDARY: { PhaseScope ph(s, PH_OTHER); TSG_LAUNCH(k_enforce32, nblk(k.nd), TPB, s, k, p); break; }
+    case TSG_RK_INIT: { PhaseScope ph(s, PH_INTEGRATE); TSG_LAUNCH(k_rk_init32, nblk(k.nd), TPB, s, k, p, st.T); break; }
+    case TSG_RK_STAGE: { PhaseScope ph(s, PH_INTEGRATE); TSG_LAUNCH(k_rk_stage32, nblk(k.nd), TPB, s, k, p, st.T); break; }
+    case TSG_RK_FINAL: { PhaseScope ph(s, PH_INTEGRATE); TSG_LAUNCH(k_rk_final32, nblk(k.nd), TPB, s, k, p, st.T, st.err); break; }
     default: break;
     }
 }
 
-void fp32_rk_update(Fp32State&, int, cudaStream_t) {}
+void fp32_rk_update(Fp32State& st, int m, cudaStream_t s) {
+    PhaseScope ph(s, PH_INTEGRATE);
+    TSG_LAUNCH(k_rk_update32, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T, (float)m);
+}
 
 // ---------------------------------------------------------------- captured steps
 // One SPHBase.step() after the (conditional) re-sort: kernel correction, init_real2tmp,
@@ -1764,12 +1852,23 @@ void fp32_rk_update(Fp32State&, int, cudaStream_t) {}
 void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
     fp32_kernel_corr(st, s);
     fp32_init_tmp(st, s);
-    fp32_one_step(st, s);
-    if (st.c.ti == 2) {
-        fp32_advect(st, TSG_ADVECT_LF_HALF, s);
+    if (st.c.ti == 4) {
+        fp32_advect(st, TSG_RK_INIT, s);
+        const int m[4] = {1, 2, 2, 1};
+        for (int q = 0; q < 4; ++q) {
+            fp32_one_step(st, s);
+            fp32_rk_update(st, m[q], s);
+            if (q < 3) fp32_advect(st, TSG_RK_STAGE, s);
+        }
+        fp32_advect(st, TSG_RK_FINAL, s);
+    } else {
         fp32_one_step(st, s);
+        if (st.c.ti == 2) {
+            fp32_advect(st, TSG_ADVECT_LF_HALF, s);
+            fp32_one_step(st, s);
+        }
+        fp32_advect(st, TSG_ADVECT_FULL, s);
     }
-    fp32_advect(st, TSG_ADVECT_FULL, s);
     fp32_advect(st, TSG_ADVECT_POS, s);
     fp32_advect(st, TSG_ADVECT_SOMETHING, s);
     if (collide) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);

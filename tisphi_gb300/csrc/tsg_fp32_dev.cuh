@@ -24,7 +24,7 @@ struct K32 {
     double vs[3], grid;
     float Q, inv_grid, h1, kk, kk6, wgrad, cub1, cub2, R2, R2lo, R2hi, pf_lim;
     float R2L, R2Lhi, disp2_limit;  // list radius (support + skin) and rebuild threshold
-    float visc_fac, eps_h2, rho0, B, gamma, dt, hdt, g[3], rep_fac, diam, h075, r_eps;
+    float visc_fac, eps_h2, rho0, B, gamma, dt, hdt, dt6, g[3], rep_fac, diam, h075, r_eps;
     float ds[3], de[3];
     // granular solvers (mu(I): mu, c2, coh; Drucker-Prager: alpha ... twoG; both: damping)
     float mu, c2, coh, alpha, k_c, kc_over_alpha, Gm, Km, sin_dila, lam_den, three_aK, nine_K_sin, twoG;
@@ -274,6 +274,10 @@ struct T32 {
     float* dee;     // d_strain_equ
     float* deep;    // d_strain_equ_p (Drucker-Prager)
     float4* vtlo;   // v_tmp low part (zero for dummies)
+    // RK4 accumulators (time_integration 4 only)
+    float* ddrk;
+    float4* dvrk;
+    float* dsigrk;  // 6 planes (Drucker-Prager)
 };
 
 // Compensated velocities of the granular solvers.  The strain rate of mu(I) is regularised
