@@ -281,7 +281,8 @@ def measure(args, cfg_dict, precision, rank, dist):
                 ps.write_field(k, host[k])
             solver.step()
             for k in outs:
-                ps.read_field(k, host[k])
+                ps.read_field(k, host[k], non_blocking=True)
+            torch.cuda.synchronize()  # the step's results are on the host before the next step
         torch.cuda.synchronize()
         el = max_over_ranks(dist, time.perf_counter() - t0)
         h2d = sum(host[k].numel() * 8 for k in ins)

@@ -203,7 +203,9 @@ int tsg_last_error(tsg_handle* h, void* stream);
  * (cell-sorted) particle order.  The caller buffer is row-major (n, k) f64 for float fields
  * and int32 for integer fields; host buffers should be pinned for the copies to overlap.
  * Replaces the reference's from_numpy / to_numpy transfers (eng/particle_system.py:289-314,
- * :413-456).  tsg_read synchronises the stream when the destination is on the host. */
+ * :413-456).  tsg_read's to_device: 0 host destination (synchronises the stream), 1 device
+ * destination, 2 host destination without synchronising (several reads can then share one
+ * synchronisation; the caller synchronises the stream before touching dst). */
 int tsg_write(tsg_handle* h, const char* name, const void* src, int from_device, void* stream);
 int tsg_read(tsg_handle* h, const char* name, void* dst, int to_device, void* stream);
 

@@ -558,13 +558,14 @@ int tsg_write(tsg_handle* h, const char* name, const void* src, int from_device,
 int tsg_read(tsg_handle* h, const char* name, void* dst, int to_device, void* stream) {
     if (!h || !name || !dst || !h->uploaded) return TSG_E_ARG;
     cudaStream_t s = S(stream);
-    if (use_fp32(h)) return fp32_read(*h->f32, name, dst, to_device != 0, s);
+    if (to_device < 0 || to_device > 2) return TSG_E_ARG;
+    if (use_fp32(h)) return fp32_read(*h->f32, name, dst, to_device, s);
     void* ptr;
     int comps, is_int;
     int rc = planar_field(h, name, &ptr, &comps, &is_int);
     if (rc) return rc;
     const size_t n = h->n;
-    const cudaMemcpyKind kind = to_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const cudaMemcpyKind kind = to_device == 1 ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     if (is_int) {
         cudaMemcpyAsync(dst, ptr, sizeof(int) * n, kind, s);
     } else if (comps == 1) {
@@ -573,7 +574,7 @@ int tsg_read(tsg_handle* h, const char* name, void* dst, int to_device, void* st
         TSG_LAUNCH(k_interleave, nb256(n), 256, s, static_cast<const double*>(ptr), h->d_stage, (int)n, comps);
         cudaMemcpyAsync(dst, h->d_stage, sizeof(double) * n * comps, kind, s);
     }
-    if (!to_device) cudaStreamSynchronize(s);
+    if (to_device == 0) cudaStreamSynchronize(s);
     return check_cuda();
 }
 

@@ -974,49 +974,52 @@ __global__ void k_enforce32(K32 k, P32 p) {
 }
 
 // ---------------------------------------------------------------- export / diagnostics
-__global__ void k_export(K32 k, P32 p, T32 t, int what, double* out) {
+// Export of one field in f64: component q of particle i goes to out[q * sq + i * si]
+// (planar views: sq = n, si = 1; row-major host buffers: sq = 1, si = components).
+__global__ void k_export(K32 k, P32 p, T32 t, int what, double* out, size_t sq, size_t si) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     const size_t n = k.n;
+    double* o = out + (size_t)i * si;
     switch (what) {
     case 0: {  // x
         float4 h = p.hi[i], l = p.lo[i];
-        out[i] = k.vs[0] + ((double)h.x + (double)l.x);
-        out[n + i] = k.vs[1] + ((double)h.y + (double)l.y);
-        out[2 * n + i] = k.vs[2] + ((double)h.z + (double)l.z);
+        o[0] = k.vs[0] + ((double)h.x + (double)l.x);
+        o[sq] = k.vs[1] + ((double)h.y + (double)l.y);
+        o[2 * sq] = k.vs[2] + ((double)h.z + (double)l.z);
         break;
     }
     case 1: {
         const float4 v = p.vel[i];
         const float4 vl = p.vlo ? p.vlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        out[i] = (double)v.x + vl.x; out[n + i] = (double)v.y + vl.y; out[2 * n + i] = (double)v.z + vl.z;
+        o[0] = (double)v.x + vl.x; o[sq] = (double)v.y + vl.y; o[2 * sq] = (double)v.z + vl.z;
         break;
     }
-    case 2: out[i] = tf_type(p.lo[i].w) > 0 ? (double)k.rho0 + (double)p.drho[i] : 0.0; break;  // density
-    case 3: out[i] = p.vel[i].w; break;                       // pressure
-    case 4: out[i] = p.hi[i].w; break;                        // m_V
-    case 5: out[i] = p.mass[i]; break;                        // mass
+    case 2: o[0] = tf_type(p.lo[i].w) > 0 ? (double)k.rho0 + (double)p.drho[i] : 0.0; break;  // density
+    case 3: o[0] = p.vel[i].w; break;                       // pressure
+    case 4: o[0] = p.hi[i].w; break;                        // m_V
+    case 5: o[0] = p.mass[i]; break;                        // mass
     case 6: {  // v_tmp
         const float4 v = t.vt[i];
         const float4 vl = t.vtlo ? t.vtlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        out[i] = (double)v.x + vl.x; out[n + i] = (double)v.y + vl.y; out[2 * n + i] = (double)v.z + vl.z;
+        o[0] = (double)v.x + vl.x; o[sq] = (double)v.y + vl.y; o[2 * sq] = (double)v.z + vl.z;
         break;
     }
-    case 7: out[i] = (double)k.rho0 + (double)t.drt[i]; break;  // density_tmp
-    case 8: out[i] = t.dd[i]; break;
-    case 9: { float4 v = t.dv[i]; out[i] = v.x; out[n + i] = v.y; out[2 * n + i] = v.z; break; }
-    case 10: out[i] = t.cf[i]; break;
-    case 11: for (int q = 0; q < 9; ++q) out[(size_t)q * n + i] = t.L ? t.L[(size_t)q * n + i] : 0.0; break;
-    case 12: case 13: case 14: {  // stress, stress_tmp, d_stress: full 3 x 3 planes from the six stored
+    case 7: o[0] = (double)k.rho0 + (double)t.drt[i]; break;  // density_tmp
+    case 8: o[0] = t.dd[i]; break;
+    case 9: { float4 v = t.dv[i]; o[0] = v.x; o[sq] = v.y; o[2 * sq] = v.z; break; }
+    case 10: o[0] = t.cf[i]; break;
+    case 11: for (int q = 0; q < 9; ++q) o[q * sq] = t.L ? t.L[(size_t)q * n + i] : 0.0; break;
+    case 12: case 13: case 14: {  // stress, stress_tmp, d_stress: full 3 x 3 from the six stored
         const float* a = what == 12 ? p.sig : what == 13 ? t.sigt : t.dsig;
         for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) out[(size_t)(3 * r + c) * n + i] = a[(size_t)sym_idx(r, c) * n + i];
+            for (int c = 0; c < 3; ++c) o[(size_t)(3 * r + c) * sq] = a[(size_t)sym_idx(r, c) * n + i];
         break;
     }
-    case 15: out[i] = p.eeq[i]; break;
-    case 16: out[i] = p.eeqp[i]; break;
-    case 17: out[i] = t.dee[i]; break;
-    case 18: out[i] = t.deep[i]; break;
+    case 15: o[0] = p.eeq[i]; break;
+    case 16: o[0] = p.eeqp[i]; break;
+    case 17: o[0] = t.dee[i]; break;
+    case 18: o[0] = t.deep[i]; break;
     default: break;
     }
 }
@@ -1037,21 +1040,24 @@ __global__ void k_export_int(K32 k, P32 p, int what, int* out) {
 }
 
 // Write a field from planar f64 staging (tsg_write).
+// Import of one field from a row-major f64 buffer (component q of particle i at
+// in[i * comps + q]).
 __global__ void k_import(K32 k, P32 p, int what, const double* in) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
-    const size_t n = k.n;
     switch (what) {
     case 0: {
+        const double* r = in + 3 * (size_t)i;
         float4 h = p.hi[i], l = p.lo[i];
-        double x[3] = {in[i] - k.vs[0], in[n + i] - k.vs[1], in[2 * n + i] - k.vs[2]};
+        double x[3] = {r[0] - k.vs[0], r[1] - k.vs[1], r[2] - k.vs[2]};
         l.x = (float)(x[0] - (double)h.x); l.y = (float)(x[1] - (double)h.y); l.z = (float)(x[2] - (double)h.z);
         p.lo[i] = l;
         break;
     }
     case 1: {
         float4 v = p.vel[i];
-        const double a = in[i], b = in[n + i], c = in[2 * n + i];
+        const double* r = in + 3 * (size_t)i;
+        const double a = r[0], b = r[1], c = r[2];
         v.x = (float)a; v.y = (float)b; v.z = (float)c;
         p.vel[i] = v;
         if (p.vlo) p.vlo[i] = make_float4((float)(a - v.x), (float)(b - v.y), (float)(c - v.z), 0.f);
@@ -1142,18 +1148,6 @@ __global__ void k_load_stress32(K32 k, const double* __restrict__ st, const int*
     p.sig[3 * n + i] = (float)a[1];
     p.sig[4 * n + i] = (float)a[2];
     p.sig[5 * n + i] = (float)a[5];
-}
-
-__global__ void k_deinterleave32(const double* src, double* dst, int n, int k) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    for (int q = 0; q < k; ++q) dst[(size_t)q * n + i] = src[(size_t)i * k + q];
-}
-
-__global__ void k_interleave32(const double* src, double* dst, int n, int k) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    for (int q = 0; q < k; ++q) dst[(size_t)i * k + q] = src[(size_t)q * n + i];
 }
 
 // Inspection: enumerate every neighbour directly (independent of the ELL capacity).
@@ -2178,6 +2172,24 @@ int fp32_autotune(Fp32State& st, int trial_steps, bool collide, cudaStream_t s, 
     return rc ? rc : (cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA);
 }
 
+namespace {
+// Float field code of k_export for a name this state keeps (-1: integer field or unknown).
+int fp32_float_field(Fp32State& st, const char* name) {
+    static const char* names[] = {"x", "v", "density", "pressure", "m_V", "mass", "v_tmp", "density_tmp",
+                                  "d_density", "d_vel", "CSPM_f", "CSPM_L", "stress", "stress_tmp", "d_stress",
+                                  "strain_equ", "strain_equ_p", "d_strain_equ", "d_strain_equ_p"};
+    for (int q = 0; q < (int)(sizeof(names) / sizeof(names[0])); ++q) {
+        if (std::strcmp(name, names[q]) != 0) continue;
+        if (q == 11 && !st.T.L) return -1;
+        if (q >= 12 && !st.P[0].sig) return -1;
+        if ((q == 14 || q == 16 || q == 18) && !st.T.dsig) return -1;
+        return q;
+    }
+    return -1;
+}
+int fp32_field_comps(int what) { return (what == 0 || what == 1 || what == 6 || what == 9) ? 3 : (what == 11 || (what >= 12 && what <= 14)) ? 9 : 1; }
+}  // namespace
+
 int fp32_field(Fp32State& st, const char* name, tsg_view* out, cudaStream_t s) {
     const std::string f(name);
     struct Spec { const char* nm; int what; int comps; int is_int; };
@@ -2205,7 +2217,7 @@ int fp32_field(Fp32State& st, const char* name, tsg_view* out, cudaStream_t s) {
         st.views.push_back({f, buf});
     }
     if (sp->is_int) TSG_LAUNCH(k_export_int, nblk(st.n), TPB, s, st.k, st.P[st.cur], sp->what, reinterpret_cast<int*>(buf));
-    else TSG_LAUNCH(k_export, nblk(st.n), TPB, s, st.k, st.P[st.cur], st.T, sp->what, buf);
+    else TSG_LAUNCH(k_export, nblk(st.n), TPB, s, st.k, st.P[st.cur], st.T, sp->what, buf, (size_t)st.n, (size_t)1);
     const int64_t n = st.n;
     out->data = buf;
     out->dtype = sp->is_int ? 2 : 0;
@@ -2251,27 +2263,27 @@ int fp32_write(Fp32State& st, const char* name, const void* src, bool from_devic
     else return TSG_E_NAME;
     const size_t n = st.n;
     double* buf = st.stage;
-    cudaMemcpyAsync(buf + 3 * n, src, sizeof(double) * comps * n, from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
-    TSG_LAUNCH(k_deinterleave32, nblk(n), TPB, s, buf + 3 * n, buf, (int)n, comps);
+    cudaMemcpyAsync(buf, src, sizeof(double) * comps * n, from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
     TSG_LAUNCH(k_import, nblk(n), TPB, s, st.k, st.P[st.cur], what, buf);
     if (what == 0) st.lists_valid = false;
     return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
 }
 
-int fp32_read(Fp32State& st, const char* name, void* dst, bool to_device, cudaStream_t s) {
-    tsg_view v;
-    int rc = fp32_field(st, name, &v, s);
-    if (rc) return rc;
+int fp32_read(Fp32State& st, const char* name, void* dst, int mode, cudaStream_t s) {
     const size_t n = st.n;
-    const int comps = v.ndim == 1 ? 1 : (v.ndim == 2 ? 3 : 9);
-    const cudaMemcpyKind kind = to_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    if (comps == 1) {
-        cudaMemcpyAsync(dst, v.data, (v.dtype == 2 ? sizeof(int) : sizeof(double)) * n, kind, s);
-    } else {
-        TSG_LAUNCH(k_interleave32, nblk(n), TPB, s, static_cast<const double*>(v.data), st.stage, (int)n, comps);
+    const cudaMemcpyKind kind = mode == 1 ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const int what = fp32_float_field(st, name);
+    if (what >= 0) {  // float fields: export straight into row-major staging, one copy
+        const int comps = fp32_field_comps(what);
+        TSG_LAUNCH(k_export, nblk(n), TPB, s, st.k, st.P[st.cur], st.T, what, st.stage, (size_t)1, (size_t)comps);
         cudaMemcpyAsync(dst, st.stage, sizeof(double) * n * comps, kind, s);
+    } else {
+        tsg_view v;
+        int rc = fp32_field(st, name, &v, s);
+        if (rc) return rc;
+        cudaMemcpyAsync(dst, v.data, sizeof(int) * n, kind, s);
     }
-    if (!to_device) cudaStreamSynchronize(s);
+    if (mode == 0) cudaStreamSynchronize(s);
     return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
 }
 

@@ -60,6 +60,8 @@ void fp32_free_adjoint(Fp32State& st);
 // Per-scene diagnostics of a batched ensemble (host out, 8 values per scene).
 int fp32_batch_diag(Fp32State& st, double pitch, double* host_out, int nscenes, cudaStream_t s);
 int fp32_write(Fp32State& st, const char* name, const void* src, bool from_device, cudaStream_t s);
-int fp32_read(Fp32State& st, const char* name, void* dst, bool to_device, cudaStream_t s);
+// mode: 0 host destination (synchronises), 1 device destination, 2 host destination
+// without synchronising (the caller synchronises the stream before using dst).
+int fp32_read(Fp32State& st, const char* name, void* dst, int mode, cudaStream_t s);
 
 }  // namespace tsg

@@ -140,15 +140,19 @@ class ParticleSystem:
             ptr, dev = src.ctypes.data, 0
         nat.check(self._lib.tsg_write(self._h, name.encode(), ctypes.c_void_p(ptr), dev, _stream()), f"write {name}")
 
-    def read_field(self, name, dst):
-        """Copy a field into a row-major (n, k) buffer (numpy array or torch tensor, host or CUDA)."""
+    def read_field(self, name, dst, non_blocking=False):
+        """Copy a field into a row-major (n, k) buffer (numpy array or torch tensor, host or CUDA).
+        non_blocking (host buffers): return without synchronising - the copy completes in
+        stream order, so synchronise (torch.cuda.synchronize) before reading dst; use pinned
+        memory."""
         if isinstance(dst, torch.Tensor):
             assert dst.is_contiguous()
             ptr, dev = dst.data_ptr(), int(dst.is_cuda)
         else:
             assert dst.flags.c_contiguous
             ptr, dev = dst.ctypes.data, 0
-        nat.check(self._lib.tsg_read(self._h, name.encode(), ctypes.c_void_p(ptr), dev, _stream()), f"read {name}")
+        mode = dev if dev or not non_blocking else 2
+        nat.check(self._lib.tsg_read(self._h, name.encode(), ctypes.c_void_p(ptr), mode, _stream()), f"read {name}")
         return dst
 
     @property
