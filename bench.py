@@ -497,6 +497,11 @@ def run_adjoint(args):
     build_native.build()
     from tisphi_gb300.adjoint import MuIRollout, distal_loss, rollout_positions
     d = scenes.column_2d(method=2, spacing=0.002, dt=2e-5)
+    # warm-up: first launches of every kernel, graph captures, allocator growth
+    warm = MuIRollout(d, nsteps=20, checkpoint_every=10)
+    wp = torch.tensor([21.9, 0.0], dtype=torch.float64, requires_grad=True)
+    distal_loss(warm(wp))[0].backward()
+    del warm
     runs = []
     for steps in sorted({200, args.adjoint_steps}):
         model = MuIRollout(d, nsteps=steps, checkpoint_every=100)
