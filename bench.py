@@ -345,6 +345,33 @@ def error_report(cfg_dict, checkpoints=(1, 20)):
             **out}
 
 
+def full_run(cfg_dict, nsteps=1000):
+    """The benchmark configuration's whole run (1,000 leap-frog steps from rest) in the
+    FP32-mixed form, timed with CUDA events: the per-step cost including every neighbour-list
+    rebuild the run needs (the K-step window of the headline starts from rest, where no
+    rebuild is due yet)."""
+    import torch
+
+    from tisphi_gb300.configer_builder import SimConfiger
+    from tisphi_gb300.simulation import Simulation
+    sim = Simulation(SimConfiger(config=cfg_dict), precision="fp32_mixed")
+    stream = torch.cuda.current_stream()
+    sim.solver.step(1)
+    torch.cuda.synchronize()
+    b0 = sim.ps.list_stats()["builds"]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    sim.solver.step(nsteps - 1)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(stop) / (nsteps - 1)
+    sim.ps.check_errors()
+    rebuilds = sim.ps.list_stats()["builds"] - b0
+    n_fluid = int(np.count_nonzero(sim.ps.scene.mat_type == 1))
+    return {"steps": nsteps, "ms_per_step": ms, "value": n_fluid / (ms * 1e-3), "list_rebuilds": rebuilds,
+            "front": sim.ps.diagnostics()["front"]}
+
+
 def read_profile_traffic(kernel_tag):
     """Per-launch DRAM bytes from a committed ncu summary (profiles/*.md), or None."""
     path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
@@ -416,6 +443,8 @@ def run_ours(args):
     }
     if "fp32_mixed" in forms and "fp64" in forms and "value" in forms["fp32_mixed"] and "value" in forms["fp64"]:
         line["speedup_fp32_mixed_vs_fp64"] = forms["fp32_mixed"]["value"] / forms["fp64"]["value"]
+    if rank == 0 and head == "fp32_mixed" and args.workload == "3d":
+        line["forms"]["fp32_mixed"]["full_1000_step_run"] = full_run(cfg_dict)
     if rank == 0 and not args.no_errors and all("value" in forms.get(p, {}) for p in ("fp32_mixed", "fp64")):
         line["errors"] = error_report(cfg_dict)
         rel = line["errors"]["after_1_steps"].get("density", {}).get("max_rel")

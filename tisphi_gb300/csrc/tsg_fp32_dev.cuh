@@ -187,11 +187,14 @@ __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restr
         const float4 hi_i = HI[i], lo_i = LO[i];
         const size_t stride = (size_t)k.n;
         const int* lp = nbr + i;
-        // two neighbours per trip: both index loads, then both position loads, then compute
+        // two neighbours per trip; the next trip's two list entries are loaded before this
+        // trip's gathers, so the entry stream (from DRAM) overlaps the gathers and the maths
         int s = 0;
+        int j0 = 0, j1 = 0;
+        if (m > 1) { j0 = lp[0]; j1 = lp[stride]; lp += 2 * stride; }
         for (; s + 1 < m; s += 2) {
-            const int j0 = lp[0], j1 = lp[stride];
-            lp += 2 * stride;
+            int n0 = 0, n1 = 0;
+            if (s + 3 < m) { n0 = lp[0]; n1 = lp[stride]; lp += 2 * stride; }
             const float4 h0 = HI[j0], l0 = LO[j0], h1 = HI[j1], l1 = LO[j1];
             float d0[3], d1[3];
             delta<DIM>(hi_i, lo_i, h0, l0, d0);
@@ -201,9 +204,11 @@ __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restr
             if (DIM == 3) { r20 += d0[2] * d0[2]; r21 += d1[2] * d1[2]; }
             if (r20 < k.R2) body(j0, d0, r20, s);        // lists hold support + skin
             if (r21 < k.R2) body(j1, d1, r21, s + 1);
+            j0 = n0;
+            j1 = n1;
         }
         if (s < m) {
-            const int j = lp[0];
+            const int j = nbr[(size_t)s * stride + i];
             float d[3];
             delta<DIM>(hi_i, lo_i, HI[j], LO[j], d);
             float r2 = d[0] * d[0] + d[1] * d[1];
