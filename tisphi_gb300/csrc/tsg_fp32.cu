@@ -281,28 +281,31 @@ __global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float
     }
 }
 
+// Inverse of the CSPM matrix (2D: the 2 x 2 block, zero (2, 2) entry; identity when
+// |det| <= 1e-8, eng/solver_sph_base.py:400-423), in f32 like the rest of this form.
 template <int DIM>
-__device__ __forceinline__ void inv_store(const K32& k, float* L, int i, const double* m, bool flow_i) {
-    double inv[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+__device__ __forceinline__ void inv_store(const K32& k, float* L, int i, const float* m, bool flow_i) {
+    float inv[9] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
     if (flow_i) {
         if (DIM == 2) {
-            double dt = m[0] * m[4] - m[1] * m[3];
-            if (fabs(dt) > EPS) {
-                double id = 1.0 / dt;
-                inv[0] = id * m[4]; inv[1] = -id * m[1]; inv[3] = -id * m[3]; inv[4] = id * m[0]; inv[8] = 0.0;
+            const float dt = m[0] * m[4] - m[1] * m[3];
+            if (fabsf(dt) > (float)EPS) {
+                const float id = 1.f / dt;
+                inv[0] = id * m[4]; inv[1] = -id * m[1]; inv[3] = -id * m[3]; inv[4] = id * m[0]; inv[8] = 0.f;
             }
         } else {
-            double dt = m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) + m[6] * (m[1] * m[5] - m[4] * m[2]);
-            if (fabs(dt) > EPS) {
-                double id = 1.0 / dt;
+            const float dt = m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) +
+                             m[6] * (m[1] * m[5] - m[4] * m[2]);
+            if (fabsf(dt) > (float)EPS) {
+                const float id = 1.f / dt;
                 for (int a = 0; a < 3; ++a)
                     for (int b = 0; b < 3; ++b)
-                        inv[3 * b + a] = id * (m[3 * ((a + 1) % 3) + (b + 1) % 3] * m[3 * ((a + 2) % 3) + (b + 2) % 3]
-                                             - m[3 * ((a + 2) % 3) + (b + 1) % 3] * m[3 * ((a + 1) % 3) + (b + 2) % 3]);
+                        inv[3 * b + a] = id * (m[3 * ((a + 1) % 3) + (b + 1) % 3] * m[3 * ((a + 2) % 3) + (b + 2) % 3] -
+                                               m[3 * ((a + 2) % 3) + (b + 1) % 3] * m[3 * ((a + 1) % 3) + (b + 2) % 3]);
             }
         }
     }
-    for (int q = 0; q < 9; ++q) L[(size_t)q * k.n + i] = (float)inv[q];
+    for (int q = 0; q < 9; ++q) L[(size_t)q * k.n + i] = inv[q];
 }
 
 // CSPM (eng/solver_sph_base.py:386-423).
@@ -330,11 +333,7 @@ __global__ void k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, con
         });
         const float sum = s.get();
         t.cf[i] = sum != 0.f ? 1.f / sum : 1.f;
-        if (k.corr == 1) {
-            double m[9];
-            for (int q = 0; q < 9; ++q) m[q] = L[q];
-            inv_store<DIM>(k, t.L, i, m, want_L);
-        }
+        if (k.corr == 1) inv_store<DIM>(k, t.L, i, L, want_L);
     });
 }
 
