@@ -83,7 +83,7 @@ __device__ __forceinline__ bool pair(const K32& k, const Start& S, int a, int b,
 template <class F>
 __device__ __forceinline__ void for_list(const K32& k, const T32& t, int i, F&& body) {
     const int m = t.cnt[i];
-    for (int s = 0; s < m; ++s) body(t.nbr[(size_t)s * k.n + i]);
+    for (int s = 0; s < m; ++s) body(entry_index(k, t.nbr[(size_t)s * k.n + i]));
 }
 
 __device__ __forceinline__ void sym2(const T32& t, size_t n, int i, float& xx, float& yy, float& xy) {
@@ -102,7 +102,7 @@ __global__ void k_adj_init(K32 k, P32 p, T32 t, Start S, A32 A, const double* __
     A.x[i] = A.v[i] = A.dv[i] = A.vn[i] = A.b1[i] = f2(0.f, 0.f);
     A.r[i] = A.mv[i] = A.rt[i] = A.dr[i] = A.b2[i] = A.bs[i] = A.dds[i] = 0.f;
     A.s[i] = A.b3[i] = A.vg[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (soil(S.lo[i].w)) {
+    if (soil(S.hi[i].w)) {
         const float2 xb = f2((float)ax[3 * (size_t)c], (float)ax[3 * (size_t)c + 1]);
         const float2 vb = f2((float)av[3 * (size_t)c], (float)av[3 * (size_t)c + 1]);
         const float rb = (float)ar[c];
@@ -128,12 +128,12 @@ __global__ void k_adj_mom(K32 k, P32 p, T32 t, Start S, A32 A) {
     const int kk = blockIdx.x * blockDim.x + threadIdx.x;
     if (kk >= k.n) return;
     const size_t n = k.n;
-    const bool ks = soil(S.lo[kk].w);
+    const bool ks = soil(S.hi[kk].w);
     float sxx, syy, sxy;
     sym2(t, n, kk, sxx, syy, sxy);
     const float rtk = k.rho0 + t.drt[kk];
     const float irk = 1.f / (rtk * rtk);
-    const float mvk = S.hi[kk].w;
+    const float mvk = S.lo[kk].w;
     const float2 ak = A.dv[kk];
     float2 ax = f2(0.f, 0.f);
     float4 as = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -141,13 +141,13 @@ __global__ void k_adj_mom(K32 k, P32 p, T32 t, Start S, A32 A) {
     for_list(k, t, kk, [&](int j) {
         Pair P;
         if (!pair(k, S, kk, j, P)) return;
-        const bool js = soil(S.lo[j].w);
+        const bool js = soil(S.hi[j].w);
         if (!ks && !js) return;
         float jxx, jyy, jxy;
         sym2(t, n, j, jxx, jyy, jxy);
         const float rtj = k.rho0 + t.drt[j];
         const float irj = 1.f / (rtj * rtj);
-        const float mvj = S.hi[j].w;
+        const float mvj = S.lo[j].w;
         // M = s~_j / rho~_j^2 + s~_k / rho~_k^2 (symmetric in the pair)
         const float Mxx = jxx * irj + sxx * irk, Myy = jyy * irj + syy * irk, Mxy = jxy * irj + sxy * irk;
         if (ks) {  // k is the centre, j the neighbour: g = G d, d = x_k - x_j
@@ -195,7 +195,7 @@ __global__ void k_adj_mom(K32 k, P32 p, T32 t, Start S, A32 A) {
 // ---- K3: boundary extrapolation reversed at each dummy (sums recomputed) ----
 __global__ void k_adj_bdy(K32 k, P32 p, T32 t, Start S, A32 A) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= k.n || soil(S.lo[b].w) || tf_type(S.lo[b].w) > 0) return;
+    if (b >= k.n || soil(S.hi[b].w) || tf_type(S.hi[b].w) > 0) return;
     const size_t n = k.n;
     float2 B1 = f2(0.f, 0.f);
     float B2 = 0.f, b1 = 0.f, b2 = 0.f;
@@ -204,8 +204,8 @@ __global__ void k_adj_bdy(K32 k, P32 p, T32 t, Start S, A32 A) {
         float d[3];
         delta<2>(S.hi[b], S.lo[b], S.hi[j], S.lo[j], d);
         const float r2 = d[0] * d[0] + d[1] * d[1];
-        if (!(r2 < k.R2) || !soil(S.lo[j].w)) return;
-        const float mw = S.hi[j].w * w_val(k, fast_sqrt(r2));
+        if (!(r2 < k.R2) || !soil(S.hi[j].w)) return;
+        const float mw = S.lo[j].w * w_val(k, fast_sqrt(r2));
         const float4 v = S.vel[j];
         const float rho = k.rho0 + S.drho[j];
         float jxx, jyy, jxy;
@@ -234,18 +234,18 @@ __global__ void k_adj_bdy(K32 k, P32 p, T32 t, Start S, A32 A) {
 // ---- K4: boundary sums' terms gathered at each soil particle ----
 __global__ void k_adj_bdy_soil(K32 k, P32 p, T32 t, Start S, A32 A) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= k.n || !soil(S.lo[j].w)) return;
+    if (j >= k.n || !soil(S.hi[j].w)) return;
     const size_t n = k.n;
     float jxx, jyy, jxy;
     sym2(t, n, j, jxx, jyy, jxy);
-    const float mvj = S.hi[j].w;
+    const float mvj = S.lo[j].w;
     const float4 v = S.vel[j];
     const float rho = k.rho0 + S.drho[j];
     float2 ax = f2(0.f, 0.f), av = f2(0.f, 0.f);
     float4 as = make_float4(0.f, 0.f, 0.f, 0.f);
     float amv = 0.f, ar = 0.f;
     for_list(k, t, j, [&](int b) {
-        if (tf_type(S.lo[b].w) > 0) return;
+        if (tf_type(S.hi[b].w) > 0) return;
         float d[3];
         delta<2>(S.hi[b], S.lo[b], S.hi[j], S.lo[j], d);  // d_bj = x_b - x_j
         const float r2 = d[0] * d[0] + d[1] * d[1];
@@ -281,7 +281,7 @@ struct Vc {
     float hx, hy, lx, ly;
 };
 __device__ __forceinline__ Vc vt_start(const Start& S, int j) {
-    if (soil(S.lo[j].w)) return {S.vel[j].x, S.vel[j].y, S.vlo[j].x, S.vlo[j].y};
+    if (soil(S.hi[j].w)) return {S.vel[j].x, S.vel[j].y, S.vlo[j].x, S.vlo[j].y};
     return {S.vt[j].x, S.vt[j].y, 0.f, 0.f};
 }
 __device__ __forceinline__ float2 vdiff(const Vc& a, const Vc& b) {  // a - b
@@ -294,13 +294,13 @@ __global__ void k_adj_stress(K32 k, P32 p, T32 t, Start S, A32 A) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     double gmu = 0.0, gcoh = 0.0;
-    if (soil(S.lo[i].w)) {
+    if (soil(S.hi[i].w)) {
         const Vc vi = vt_start(S, i);
         float vxx = 0.f, vxy = 0.f, vyx = 0.f, vyy = 0.f;
         for_list(k, t, i, [&](int j) {
             Pair P;
             if (!pair(k, S, i, j, P)) return;
-            const float mvj = S.hi[j].w;
+            const float mvj = S.lo[j].w;
             const float2 u = vdiff(vt_start(S, j), vi);
             const float ux = mvj * u.x, uy = mvj * u.y;
             const float gx = P.G * P.dx, gy = P.G * P.dy;
@@ -333,7 +333,7 @@ __global__ void k_adj_stress(K32 k, P32 p, T32 t, Start S, A32 A) {
         for_list(k, t, i, [&](int j) {
             Pair P;
             if (!pair(k, S, i, j, P)) return;
-            const float mvj = S.hi[j].w;
+            const float mvj = S.lo[j].w;
             const float2 u = vdiff(vt_start(S, j), vi);
             const float ux = u.x, uy = u.y;
             const float gx = P.G * P.dx, gy = P.G * P.dy;
@@ -381,13 +381,13 @@ __global__ void k_adj_params(int n, const double2* __restrict__ gp, double* __re
 __global__ void k_adj_vgrad(K32 k, P32 p, T32 t, Start S, A32 A) {
     const int kk = blockIdx.x * blockDim.x + threadIdx.x;
     if (kk >= k.n) return;
-    const bool ks = soil(S.lo[kk].w);
-    const float mvk = S.hi[kk].w;
+    const bool ks = soil(S.hi[kk].w);
+    const float mvk = S.lo[kk].w;
     const Vc vk = vt_start(S, kk);
     float2 av = f2(0.f, 0.f), ax = f2(0.f, 0.f);
     float amv = 0.f;
     for_list(k, t, kk, [&](int i) {
-        if (!soil(S.lo[i].w)) return;
+        if (!soil(S.hi[i].w)) return;
         Pair P;
         if (!pair(k, S, kk, i, P)) return;
         const float4 g4 = A.vg[i];
@@ -421,7 +421,7 @@ __global__ void k_adj_out(K32 k, P32 p, Start S, A32 A, double* __restrict__ ax,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     const size_t c = (size_t)p.ids[i].x;
-    if (soil(S.lo[i].w)) {
+    if (soil(S.hi[i].w)) {
         const float rho = k.rho0 + S.drho[i];
         const float r = A.r[i] - A.mv[i] * p.mass[i] / (rho * rho);
         ax[3 * c] = A.x[i].x; ax[3 * c + 1] = A.x[i].y; ax[3 * c + 2] = 0.0;

@@ -104,7 +104,7 @@ __global__ void k_reorder32(K32 k, int count_n, int base, const int* __restrict_
         b.flag[dst] = a.flag[src];
     }
     if (a.vlo) b.vlo[dst] = a.vlo[src];
-    PF[dst] = make_float4(pfv[0], pfv[1], pfv[2], l.w);
+    PF[dst] = make_float4(pfv[0], pfv[1], pfv[2], h.w);
 }
 
 // Record a particle whose neighbours exceed the list capacity (processed by FB passes).
@@ -120,9 +120,10 @@ __global__ void k_lists(K32 k, const float4* __restrict__ HI, const float4* __re
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     const bool flow_i = is_flow(tf_type(PF[i].w));
+    const float4 hi_i = HI[i];
     int m = 0;
     enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float*, float) {
-        if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
+        if (m < k.maxn) nbr[(size_t)m * k.n + i] = entry_of(k, j, hi_i, HI[j]);
         ++m;
     }, true);
     cnt[i] = m;
@@ -155,10 +156,14 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
         const int i = p0 + lane;
         const bool active = i < ce;
         float rx = 0.f, ry = 0.f, rz = 0.f;
+        int qi[3] = {0, 0, 0};  // (hi_i - ref) / Q
         bool flow_i = false, alias = false;
         if (active) {
             const float4 hi_i = HI[i], lo_i = LO[i];
-            flow_i = is_flow(tf_type(lo_i.w));
+            flow_i = is_flow(tf_type(hi_i.w));
+            qi[0] = (int)rintf((hi_i.x - ref.x) * k.inv_Q);
+            qi[1] = (int)rintf((hi_i.y - ref.y) * k.inv_Q);
+            qi[2] = (int)rintf((hi_i.z - ref.z) * k.inv_Q);
             bool ok = true;
             alias = cell_coord(k, hi_i.x, lo_i.x, ok) != cx || cell_coord(k, hi_i.y, lo_i.y, ok) != cy ||
                     cell_coord(k, hi_i.z, lo_i.z, ok) != cz || !ok;
@@ -185,8 +190,13 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
                         const int jj = base + lane;
                         if (jj < re) {
                             const float4 hj = HI[jj], lj = LO[jj];
+                            // w: material class (bits 0-2) and (hj - ref) / Q + 8 per axis (4 bits each)
+                            const int qx = (int)rintf((hj.x - ref.x) * k.inv_Q) + 8;
+                            const int qy = (int)rintf((hj.y - ref.y) * k.inv_Q) + 8;
+                            const int qz = (int)rintf((hj.z - ref.z) * k.inv_Q) + 8;
+                            const int tag = type_class(tf_type(hj.w)) | (qx << 3) | (qy << 7) | (qz << 11);
                             sh_rel[wib][lane] = make_float4((hj.x - ref.x) + lj.x, (hj.y - ref.y) + lj.y,
-                                                            (hj.z - ref.z) + lj.z, lj.w);
+                                                            (hj.z - ref.z) + lj.z, __int_as_float(tag));
                         }
                         __syncwarp();
                         const int mm = re - base < 32 ? re - base : 32;
@@ -203,14 +213,19 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
                                     const float dz = rz - q.z;
                                     r2 += dz * dz;
                                 }
-                                const bool ok_type = flow_i || is_flow(tf_type(q.w));
+                                const bool ok_type = flow_i || (__float_as_int(q.w) & 7) <= 1;
                                 acc |= (t < mm && r2 < k.R2L && ok_type) ? (1u << t) : 0u;
                             }
                             if (i >= base && i < base + 32) acc &= ~(1u << (i - base));
                             while (acc) {
                                 const int t = __ffs(acc) - 1;
                                 acc &= acc - 1u;
-                                if (m < k.maxn) { *wp = base + t; wp += stride; }
+                                if (m < k.maxn) {
+                                    const int tag = __float_as_int(sh_rel[wib][t].w);
+                                    *wp = make_entry(base + t, class_type(tag & 7), qi[0] - (((tag >> 3) & 15) - 8),
+                                                     qi[1] - (((tag >> 7) & 15) - 8), qi[2] - (((tag >> 11) & 15) - 8));
+                                    wp += stride;
+                                }
                                 ++m;
                             }
                         }
@@ -251,9 +266,10 @@ __global__ void k_lists_fixup(K32 k, const float4* __restrict__ HI, const float4
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.n; i += gridDim.x * blockDim.x) {
         if (cnt[i] >= 0) continue;
         const bool flow_i = is_flow(tf_type(PF[i].w));
+        const float4 hi_i = HI[i];
         int m = 0;
         enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float*, float) {
-            if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
+            if (m < k.maxn) nbr[(size_t)m * k.n + i] = entry_of(k, j, hi_i, HI[j]);
             ++m;
         }, true);
         cnt[i] = m;
@@ -271,9 +287,10 @@ __global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float
     const int b0 = bounds[0], b1 = bounds[1];
     for (int i = b0 + blockIdx.x * blockDim.x + threadIdx.x; i < b1; i += gridDim.x * blockDim.x) {
         const bool flow_i = is_flow(tf_type(PF[i].w));
+        const float4 hi_i = HI[i];
         int m = 0;
         enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float*, float) {
-            if (m < k.maxn) nbr[(size_t)m * k.n + i] = j;
+            if (m < k.maxn) nbr[(size_t)m * k.n + i] = entry_of(k, j, hi_i, HI[j]);
             ++m;
         }, true);
         cnt[i] = m;
@@ -313,20 +330,18 @@ template <int DIM, bool FB>
 __global__ void k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                          const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.n, ovf, t.cnt, k.maxn, {
-        const int ti = tf_type(p.lo[i].w);
+        const int ti = tf_type(p.hi[i].w);
         const bool flow_i = is_flow(ti);
         const bool want_L = k.corr == 1 && flow_i;
         CSum s;
         float L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, flow_i,
-                          [&](int j, const float* d, float r2, int sidx) {
-            const float4 hj = p.hi[j];
-            const int tj = tf_type(p.lo[j].w);
+                          [&](int j, const float* d, float r2, int sidx, int tj, float mVj) {
             const float r = fast_sqrt(r2);
-            if (is_flow(tj)) s.add(hj.w * w_val(k, r));
+            if (is_flow(tj)) s.add(mVj * w_val(k, r));
             if ((sidx & 7) == 7) s.flush();
             if (want_L && tj == ti) {
-                const float gf = w_grad(k, r) * hj.w;
+                const float gf = w_grad(k, r) * mVj;
                 for (int a = 0; a < DIM; ++a)
                     for (int b = 0; b < DIM; ++b) L[3 * a + b] += (-d[a]) * (gf * d[b]);
             }
@@ -340,7 +355,7 @@ __global__ void k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, con
 __global__ void k_init_tmp32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
-    const int ti = tf_type(p.lo[i].w);
+    const int ti = tf_type(p.hi[i].w);
     if (ti > 0) {
         const float4 v = p.vel[i];
         t.vt[i] = make_float4(v.x, v.y, v.z, t.vt[i].w);
@@ -372,7 +387,7 @@ __device__ __forceinline__ float tait(const K32& k, float drt, float B) {
 __global__ void k_pre32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const float w = p.lo[i].w;
+    const float w = p.hi[i].w;
     if (tf_type(w) != MAT_FLUID) return;
     const float drt = t.drt[i];
     const float pr = tait(k, drt, k.scene_par ? k.scene_par[tf_scene(w)].x : k.B);
@@ -388,14 +403,13 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
                         const int* __restrict__ sstart, int base, int count_n, Ovf ovf) {
     const int lim = base + count_n;
     FOR_PARTICLES(FB, base, lim, ovf, t.cnt, k.maxn, {
-        const int ti = tf_type(p.lo[i].w);
+        const int ti = tf_type(p.hi[i].w);
         if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
             CSum bv[3], bp;
             const float4 hi_i = p.hi[i], lo_i = p.lo[i];
             for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
-                              [&](int j, const float* d, float r2, int sidx) {
+                              [&](int j, const float* d, float r2, int sidx, int, float mV) {
                 const float w = w_val(k, fast_sqrt(r2));
-                const float mV = p.hi[j].w;
                 const float4 vt = t.vt[j];
                 const float2 pr = t.pr[j];
                 const float mw = mV * w;
@@ -424,7 +438,7 @@ template <int DIM, bool FB, bool CORR>
 __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                           const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
-      const float wi = p.lo[i].w;
+      const float wi = p.hi[i].w;
       if (tf_type(wi) == MAT_FLUID) {
         const float visc_fac = k.scene_par ? k.scene_par[tf_scene(wi)].y : k.visc_fac;
         const float4 vti = t.vt[i];
@@ -436,9 +450,7 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         CSum dd, dv[3];
         const bool rep_on = k.boundary == 3 || k.boundary == 4;
         for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
-                          [&](int j, const float* d, float r2, int sidx) {
-            const float4 hj = p.hi[j];
-            const int tj = tf_type(p.lo[j].w);
+                          [&](int j, const float* d, float r2, int sidx, int tj, float mVj) {
             const float4 vtj = t.vt[j];
             const float r = fast_sqrt(r2);
             const float gf = w_grad(k, r);
@@ -449,17 +461,17 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
                 const float cx = L[0] * gx + L[1] * gy + (DIM == 3 ? L[2] * gz : 0.f);
                 const float cy = L[3] * gx + L[4] * gy + (DIM == 3 ? L[5] * gz : 0.f);
                 const float cz = DIM == 3 ? L[6] * gx + L[7] * gy + L[8] * gz : 0.f;
-                dd.add(hj.w * (dvx * cx + dvy * cy + (DIM == 3 ? dvz * cz : 0.f)));
+                dd.add(mVj * (dvx * cx + dvy * cy + (DIM == 3 ? dvz * cz : 0.f)));
             } else {
-                dd.add(hj.w * (dvx * gx + dvy * gy + (DIM == 3 ? dvz * gz : 0.f)));
+                dd.add(mVj * (dvx * gx + dvy * gy + (DIM == 3 ? dvz * gz : 0.f)));
             }
             // viscosity (fluid or boundary neighbours) and pressure, on the uncorrected gradient
             const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
             // WCSPH scenes hold fluid, dummy, repulsive and rigid particles only (soil is rejected
             // at upload), so every non-fluid neighbour takes the boundary form
-            const float cv = __fdividef(visc_fac * hj.w * fminf(vdx, 0.f), r2 + k.eps_h2) *
+            const float cv = __fdividef(visc_fac * mVj * fminf(vdx, 0.f), r2 + k.eps_h2) *
                              (tj == MAT_FLUID ? 1.f : visc_b);
-            const float cp = -k.rho0 * hj.w * (vti.w + vtj.w);
+            const float cp = -k.rho0 * mVj * (vti.w + vtj.w);
             float sc = (cv + cp) * gf;
             float rs = 0.f;
             if (rep_on && tj == MAT_REP) {  // repulsive force (eng/solver_sph_base.py:675-689)
@@ -488,7 +500,7 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
 __global__ void k_pre_dp32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    if (tf_type(p.lo[i].w) != MAT_SOIL) return;
+    if (tf_type(p.hi[i].w) != MAT_SOIL) return;
     float st[6];
     load_sym(t.sigt, k.n, i, st);
     dp_adapt32(k, st);
@@ -501,7 +513,7 @@ template <int DIM, bool FB, bool CORR>
 __global__ void k_mui_stress32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                                const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
-      if (tf_type(p.lo[i].w) == MAT_SOIL) {
+      if (tf_type(p.hi[i].w) == MAT_SOIL) {
         const float4 vti = t.vt[i], vli = t.vtlo[i];
         float L[9];
         if (CORR)
@@ -509,10 +521,10 @@ __global__ void k_mui_stress32(K32 k, P32 p, T32 t, const float4* __restrict__ P
         float vg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         CSum dd;
         for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
-                          [&](int j, const float* d, float r2, int sidx) {
+                          [&](int j, const float* d, float r2, int sidx, int, float mVj) {
             float kc[3];
             grad_c<DIM, CORR>(L, w_grad(k, fast_sqrt(r2)), d, kc);
-            vgrad_add<DIM>(p.hi[j].w, vti, vli, t.vt[j], t.vtlo[j], kc, vg, dd);
+            vgrad_add<DIM>(mVj, vti, vli, t.vt[j], t.vtlo[j], kc, vg, dd);
             if ((sidx & 7) == 7) dd.flush();
         });
         const size_t n = k.n;
@@ -537,14 +549,14 @@ __global__ void k_bdy_soil32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
                              const int* __restrict__ sstart, int base, int count_n, Ovf ovf) {
     const int lim = base + count_n;
     FOR_PARTICLES(FB, base, lim, ovf, t.cnt, k.maxn, {
-        const int ti = tf_type(p.lo[i].w);
+        const int ti = tf_type(p.hi[i].w);
         if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
             const size_t n = k.n;
             CSum bv[3], b1, b2;
             float bs[6] = {0, 0, 0, 0, 0, 0};
             for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
-                              [&](int j, const float* d, float r2, int sidx) {
-                const float mw = p.hi[j].w * w_val(k, fast_sqrt(r2));
+                              [&](int j, const float* d, float r2, int sidx, int, float mVj) {
+                const float mw = mVj * w_val(k, fast_sqrt(r2));
                 const float4 vt = t.vt[j];
                 const float drt = t.drt[j];
                 const float rtj = k.rho0 + drt;
@@ -578,7 +590,7 @@ template <int DIM, bool FB, bool CORR, bool DP>
 __global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                              const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
-      if (tf_type(p.lo[i].w) == MAT_SOIL) {
+      if (tf_type(p.hi[i].w) == MAT_SOIL) {
         const size_t n = k.n;
         const float4 vti = t.vt[i], vli = t.vtlo[i];
         float L[9];
@@ -594,8 +606,7 @@ __global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
         float vg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         const bool rep_on = k.boundary == 3 || k.boundary == 4;
         for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
-                          [&](int j, const float* d, float r2, int sidx) {
-            const float mVj = p.hi[j].w;
+                          [&](int j, const float* d, float r2, int sidx, int tj, float mVj) {
             const float rtj = k.rho0 + t.drt[j];
             const float r = fast_sqrt(r2);
             float kc[3];
@@ -618,7 +629,7 @@ __global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
                 dv[1].add(coef * (mxy * kc[0] + myy * kc[1]));
             }
             if (DP) vgrad_add<DIM>(mVj, vti, vli, t.vt[j], t.vtlo[j], kc, vg, dd);
-            if (rep_on && tf_type(p.lo[j].w) == MAT_REP) {  // eng/solver_sph_base.py:675-689
+            if (rep_on && tj == MAT_REP) {  // eng/solver_sph_base.py:675-689
                 const float chi = (r > 0.f && r < k.diam) ? 1.f - r / k.diam : 0.f;
                 const float gm = r / k.h075;
                 float fr = 0.f;
@@ -682,10 +693,10 @@ __global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
 __global__ void k_post_mui32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    if (tf_type(p.lo[i].w) != MAT_SOIL) return;
+    if (tf_type(p.hi[i].w) != MAT_SOIL) return;
     const float dr = fmaxf(p.drho[i], 0.f);
     p.drho[i] = dr;
-    p.hi[i].w = p.mass[i] / (k.rho0 + dr);
+    p.lo[i].w = p.mass[i] / (k.rho0 + dr);
     p.eeq[i] += k.dt * t.dee[i];
 }
 
@@ -698,12 +709,12 @@ template <int DIM>
 __global__ void k_reg_mui32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                             const int* __restrict__ sstart) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.nd; i += gridDim.x * blockDim.x) {
-        if (tf_type(p.lo[i].w) != MAT_SOIL) continue;
+        if (tf_type(p.hi[i].w) != MAT_SOIL) continue;
         const size_t n = k.n;
         float s[6] = {0, 0, 0, 0, 0, 0};
         enum_neighbors<DIM>(k, i, p.hi, p.lo, PF, dstart, sstart, false, [&](int j, const float*, float r2) {
-            if (tf_type(p.lo[j].w) != MAT_SOIL) return;
-            const float mw = p.hi[j].w * w_val(k, fast_sqrt(r2));
+            if (tf_type(p.hi[j].w) != MAT_SOIL) return;
+            const float mw = p.lo[j].w * w_val(k, fast_sqrt(r2));
             for (int q = 0; q < 6; ++q) s[q] += mw * t.sigt[q * n + j];
         }, false, false);
         const float f = t.cf[i];
@@ -715,10 +726,10 @@ __global__ void k_reg_mui32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, 
 __global__ void k_post_dp32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    if (tf_type(p.lo[i].w) != MAT_SOIL) return;
+    if (tf_type(p.hi[i].w) != MAT_SOIL) return;
     const float dr = fmaxf(p.drho[i], 0.f);
     p.drho[i] = dr;
-    p.hi[i].w = p.mass[i] / (k.rho0 + dr);
+    p.lo[i].w = p.mass[i] / (k.rho0 + dr);
     float st[6];
     load_sym(p.sig, k.n, i, st);
     p.flag[i] = dp_flag32(k, st);
@@ -733,14 +744,14 @@ __global__ void k_post_dp32(K32 k, P32 p, T32 t) {
 __global__ void k_ymax32(K32 k, P32 p, double* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double y = -DBL_MAX;
-    if (i < k.nd && tf_type(p.lo[i].w) == MAT_SOIL) y = k.vs[1] + ((double)p.hi[i].y + (double)p.lo[i].y);
+    if (i < k.nd && tf_type(p.hi[i].w) == MAT_SOIL) y = k.vs[1] + ((double)p.hi[i].y + (double)p.lo[i].y);
     for (int o = 16; o > 0; o >>= 1) y = fmax(y, __shfl_down_sync(0xffffffffu, y, o));
     if ((threadIdx.x & 31) == 0) atomic_max_d(out, y);
 }
 __global__ void k_geostatic32(K32 k, P32 p, const double* ymax, double K0) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    if (tf_type(p.lo[i].w) != MAT_SOIL) return;
+    if (tf_type(p.hi[i].w) != MAT_SOIL) return;
     const double y = k.vs[1] + ((double)p.hi[i].y + (double)p.lo[i].y);
     const double vs = (double)k.rho0 * (double)k.g[1] * (ymax[0] - y);
     const size_t n = k.n;
@@ -754,7 +765,7 @@ __global__ void k_geostatic32(K32 k, P32 p, const double* ymax, double K0) {
 __global__ void k_advect_half32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const int ti = tf_type(p.lo[i].w);
+    const int ti = tf_type(p.hi[i].w);
     if (ti <= 0) return;
     if (ti == MAT_SOIL && k.solver == 3) {
         const size_t n = k.n;
@@ -762,7 +773,7 @@ __global__ void k_advect_half32(K32 k, P32 p, T32 t) {
     }
     const float drt = t.drt[i] + k.hdt * t.dd[i];
     t.drt[i] = drt;
-    p.hi[i].w = p.mass[i] / (k.rho0 + drt);
+    p.lo[i].w = p.mass[i] / (k.rho0 + drt);
     const float4 dv = t.dv[i];
     float4 vt = t.vt[i];
     if (t.vtlo) {
@@ -782,7 +793,7 @@ __global__ void k_advect_half32(K32 k, P32 p, T32 t) {
 __global__ void k_rk_init32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const int ti = tf_type(p.lo[i].w);
+    const int ti = tf_type(p.hi[i].w);
     if (ti <= 0) return;
     t.ddrk[i] = 0.f;
     t.dvrk[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -793,7 +804,7 @@ __global__ void k_rk_init32(K32 k, P32 p, T32 t) {
 __global__ void k_rk_update32(K32 k, P32 p, T32 t, float m) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const int ti = tf_type(p.lo[i].w);
+    const int ti = tf_type(p.hi[i].w);
     if (ti <= 0) return;
     t.ddrk[i] += t.dd[i] * m;
     const float4 dv = t.dv[i];
@@ -807,11 +818,11 @@ __global__ void k_rk_update32(K32 k, P32 p, T32 t, float m) {
 __global__ void k_rk_stage32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const int ti = tf_type(p.lo[i].w);
+    const int ti = tf_type(p.hi[i].w);
     if (ti <= 0) return;
     const float drt = k.hdt * t.dd[i] + p.drho[i];
     t.drt[i] = drt;
-    p.hi[i].w = p.mass[i] / (k.rho0 + drt);
+    p.lo[i].w = p.mass[i] / (k.rho0 + drt);
     const float4 dv = t.dv[i];
     float4 vt = p.vel[i];
     if (t.vtlo) {
@@ -832,11 +843,11 @@ __global__ void k_rk_stage32(K32 k, P32 p, T32 t) {
 __global__ void k_rk_final32(K32 k, P32 p, T32 t, int* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const int ti = tf_type(p.lo[i].w);
+    const int ti = tf_type(p.hi[i].w);
     if (ti <= 0) return;
     const float dr = p.drho[i] + k.dt6 * t.ddrk[i];
     p.drho[i] = dr;
-    p.hi[i].w = p.mass[i] / (k.rho0 + dr);
+    p.lo[i].w = p.mass[i] / (k.rho0 + dr);
     const float4 a = t.dvrk[i];
     float4 v = p.vel[i];
     if (p.vlo) {
@@ -857,7 +868,7 @@ __global__ void k_rk_final32(K32 k, P32 p, T32 t, int* err) {
 __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const int ti = tf_type(p.lo[i].w);
+    const int ti = tf_type(p.hi[i].w);
     if (ti <= 0) return;
     if (ti == MAT_SOIL && k.solver == 3) {
         const size_t n = k.n;
@@ -865,7 +876,7 @@ __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
     }
     const float dr = p.drho[i] + k.dt * t.dd[i];
     p.drho[i] = dr;
-    p.hi[i].w = p.mass[i] / (k.rho0 + dr);
+    p.lo[i].w = p.mass[i] / (k.rho0 + dr);
     const float4 dv = t.dv[i];
     float4 v = p.vel[i];
     if (p.vlo) {
@@ -885,14 +896,14 @@ template <int DIM, bool FB>
 __global__ void k_xsph32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                          const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
-        const int ti = tf_type(p.lo[i].w);
-        if (ti > 0 && tf_dyn(p.lo[i].w)) {
+        const int ti = tf_type(p.hi[i].w);
+        if (ti > 0 && tf_dyn(p.hi[i].w)) {
             const float4 vi = p.vel[i];
             CSum s[3];
             for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, is_flow(ti),
-                              [&](int j, const float*, float r2, int sidx) {
-                if (tf_type(p.lo[j].w) != ti) return;
-                const float w = w_val(k, fast_sqrt(r2)) * p.hi[j].w;
+                              [&](int j, const float*, float r2, int sidx, int tj, float mVj) {
+                if (tj != ti) return;
+                const float w = w_val(k, fast_sqrt(r2)) * mVj;
                 const float4 vj = p.vel[j];
                 s[0].add(w * (vj.x - vi.x));
                 s[1].add(w * (vj.y - vi.y));
@@ -907,7 +918,7 @@ __global__ void k_xsph32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, con
 __global__ void k_advect_pos32(K32 k, P32 p, T32 t, int* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const float w = p.lo[i].w;
+    const float w = p.hi[i].w;
     if (tf_type(w) <= 0) return;
     float4 v = p.vel[i];
     if (p.vlo) {
@@ -932,18 +943,18 @@ __global__ void k_advect_pos32(K32 k, P32 p, T32 t, int* err) {
 __global__ void k_post_wc32(K32 k, P32 p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    if (tf_type(p.lo[i].w) != MAT_FLUID) return;
+    if (tf_type(p.hi[i].w) != MAT_FLUID) return;
     const float dr = fmaxf(p.drho[i], 0.f);
     p.drho[i] = dr;
-    p.hi[i].w = p.mass[i] / (k.rho0 + dr);
+    p.lo[i].w = p.mass[i] / (k.rho0 + dr);
 }
 
 // Collision boundary (eng/solver_sph_base.py:525-601), flow particles when boundary == 1.
 __global__ void k_enforce32(K32 k, P32 p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const int ti = tf_type(p.lo[i].w);
-    const bool rigid_dyn = ti == MAT_RIGID && tf_dyn(p.lo[i].w);
+    const int ti = tf_type(p.hi[i].w);
+    const bool rigid_dyn = ti == MAT_RIGID && tf_dyn(p.hi[i].w);
     const bool on = k.boundary == 1 ? (is_flow(ti) || rigid_dyn) : rigid_dyn;
     if (!on) return;
     float4 h = p.hi[i], l = p.lo[i];
@@ -994,9 +1005,9 @@ __global__ void k_export(K32 k, P32 p, T32 t, int what, double* out, size_t sq, 
         o[0] = (double)v.x + vl.x; o[sq] = (double)v.y + vl.y; o[2 * sq] = (double)v.z + vl.z;
         break;
     }
-    case 2: o[0] = tf_type(p.lo[i].w) > 0 ? (double)k.rho0 + (double)p.drho[i] : 0.0; break;  // density
+    case 2: o[0] = tf_type(p.hi[i].w) > 0 ? (double)k.rho0 + (double)p.drho[i] : 0.0; break;  // density
     case 3: o[0] = p.vel[i].w; break;                       // pressure
-    case 4: o[0] = p.hi[i].w; break;                        // m_V
+    case 4: o[0] = p.lo[i].w; break;                        // m_V
     case 5: o[0] = p.mass[i]; break;                        // mass
     case 6: {  // v_tmp
         const float4 v = t.vt[i];
@@ -1029,7 +1040,7 @@ __global__ void k_export_int(K32 k, P32 p, int what, int* out) {
     const int4 id = p.ids[i];
     switch (what) {
     case 0: out[i] = id.x; break;
-    case 1: out[i] = tf_type(p.lo[i].w); break;
+    case 1: out[i] = tf_type(p.hi[i].w); break;
     case 2: out[i] = id.y; break;
     case 3: out[i] = id.z; break;
     case 4: out[i] = id.w; break;
@@ -1062,7 +1073,7 @@ __global__ void k_import(K32 k, P32 p, int what, const double* in) {
         if (p.vlo) p.vlo[i] = make_float4((float)(a - v.x), (float)(b - v.y), (float)(c - v.z), 0.f);
         break;
     }
-    case 2: if (tf_type(p.lo[i].w) > 0) p.drho[i] = (float)(in[i] - (double)k.rho0); break;
+    case 2: if (tf_type(p.hi[i].w) > 0) p.drho[i] = (float)(in[i] - (double)k.rho0); break;
     case 3: p.vel[i].w = (float)in[i]; break;
     default: break;
     }
@@ -1073,7 +1084,7 @@ __global__ void k_diag32(K32 k, P32 p, double* out) {
     __shared__ double sh[8][TPB / 32];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[8] = {0, 0, 0, 0, 0, 0, 0, -DBL_MAX};
-    if (i < k.nd && is_flow(tf_type(p.lo[i].w))) {
+    if (i < k.nd && is_flow(tf_type(p.hi[i].w))) {
         const double m = p.mass[i];
         const float4 vv = p.vel[i];
         const float4 h = p.hi[i], l = p.lo[i];
@@ -1124,8 +1135,8 @@ __global__ void k_load32(K32 k, const double* __restrict__ x, const double* __re
     // bit 30 keeps the word a normal float, so no denormal flush can touch it in transit
     const int sc = scene_of ? (scene_of[s] & 0xfff) : 0;
     const int word = 0x40000000 | (mt[s] & 0xffff) | ((dyn[s] & 1) << 16) | (sc << 17);
-    p.hi[i] = make_float4(hv[0], hv[1], hv[2], (float)mV[s]);
-    p.lo[i] = make_float4(lv[0], lv[1], lv[2], __int_as_float(word));
+    p.hi[i] = make_float4(hv[0], hv[1], hv[2], __int_as_float(word));
+    p.lo[i] = make_float4(lv[0], lv[1], lv[2], (float)mV[s]);
     const double v0 = v[3 * (size_t)s], v1 = v[3 * (size_t)s + 1], v2 = v[3 * (size_t)s + 2];
     p.vel[i] = make_float4((float)v0, (float)v1, (float)v2, (float)pres[s]);
     if (p.vlo) p.vlo[i] = make_float4((float)(v0 - (float)v0), (float)(v1 - (float)v1), (float)(v2 - (float)v2), 0.f);
@@ -1178,7 +1189,7 @@ __global__ void k_nbr_count_ell(K32 k, const float4* HI, const float4* LO, const
     const int m = cnt[i] < k.maxn ? cnt[i] : k.maxn;
     int c = 0;
     for (int q = 0; q < m; ++q) {
-        const int j = nbr[(size_t)q * k.n + i];
+        const int j = entry_index(k, nbr[(size_t)q * k.n + i]);
         float d[3];
         delta<DIM>(HI[i], LO[i], HI[j], LO[j], d);
         const float r2 = d[0] * d[0] + d[1] * d[1] + (DIM == 3 ? d[2] * d[2] : 0.f);
@@ -1196,7 +1207,7 @@ __global__ void k_nbr_fill_ell(K32 k, const float4* HI, const float4* LO, const 
     int w = off[i];
     if (m <= k.maxn) {
         for (int q = 0; q < m; ++q) {
-            const int j = nbr[(size_t)q * k.n + i];
+            const int j = entry_index(k, nbr[(size_t)q * k.n + i]);
             float d[3];
             delta<DIM>(HI[i], LO[i], HI[j], LO[j], d);
             const float r2 = d[0] * d[0] + d[1] * d[1] + (DIM == 3 ? d[2] * d[2] : 0.f);
@@ -1255,7 +1266,7 @@ __global__ void k_diag_batch32(K32 k, P32 p, double pitch, double* out) {
     double v[8] = {0, 0, 0, 0, 0, 0, 0, -DBL_MAX};
     int sc = -1;
     if (i < k.nd) {
-        const float w = p.lo[i].w;
+        const float w = p.hi[i].w;
         if (is_flow(tf_type(w))) {
             sc = tf_scene(w);
             const double m = p.mass[i];
@@ -1313,10 +1324,11 @@ T* dal(Fp32State& st, size_t count) {
     return static_cast<T*>(q);
 }
 
+// Smallest power of two not below the cell size (list entries assume |hi_i - hi_j| <= Q).
 float pow2_quantum(double grid) {
     double q = 1.0;
-    while (q > grid) q *= 0.5;
-    while (q * 2.0 <= grid) q *= 2.0;
+    while (q < grid) q *= 2.0;
+    while (q * 0.5 >= grid) q *= 0.5;
     return (float)q;
 }
 
@@ -1362,6 +1374,7 @@ __global__ void k_offset(int* a, long long m, int off) {
 int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp, bool from_device,
                 Fp32State** out, cudaStream_t s, const Fp32Scenes* scenes) {
     *out = nullptr;
+    if (c.n > (1 << kEntryBits)) return TSG_E_CAPACITY;  // neighbour-list entries index 2^24 particles
 
     Fp32State* st = new Fp32State();
     st->c = c;
@@ -1415,6 +1428,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
         k.G = G;
     }
     k.Q = pow2_quantum(k.grid);
+    k.inv_Q = 1.f / k.Q;
     k.inv_grid = (float)(1.0 / k.grid);
     // host copies of the classification to place particles: dynamic block first
     std::vector<int32_t> mt(n);

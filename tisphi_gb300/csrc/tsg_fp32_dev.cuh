@@ -32,15 +32,42 @@ struct K32 {
     // batched ensembles: per-scene (stiffness B, viscosity factor), indexed by the scene
     // number in the type word; nullptr for a single scene (B and visc_fac above)
     const float2* scene_par;
+    float inv_Q;    // 1 / Q (a power of two)
 };
 
-// Type word (the w lane of lo): bits 0-15 material type (signed), bit 16 is_dynamic, bits
+// Type word (the w lane of hi): bits 0-15 material type (signed), bit 16 is_dynamic, bits
 // 17-28 scene number of a batched ensemble, bit 30 set (the word stays a normal float).
 __device__ __forceinline__ int tf_type(float w) { return (int)(short)(__float_as_int(w) & 0xffff); }
 __device__ __forceinline__ int tf_dyn(float w) { return (__float_as_int(w) >> 16) & 1; }
 __device__ __forceinline__ int tf_scene(float w) { return (__float_as_int(w) >> 17) & 0xfff; }
 constexpr int kMaxScenes = 4096;
 __device__ __forceinline__ bool is_flow(int t) { return t == MAT_FLUID || t == MAT_SOIL; }
+
+// Neighbour-list entries pack the neighbour index (bits 0-23, so this form holds at most
+// 2^24 particles), its material class (bits 24-26: fluid, soil, dummy, repulsive, rigid)
+// and the offset (hi_i - hi_j) / Q of the two particles' quantised positions (bits 27-31:
+// base-3 code of three offsets in -1..1; Q is at least one cell of the list grid, so two
+// listed particles are never more than one quantum apart, and hi only changes when the
+// lists are rebuilt).  A traversal therefore reads the neighbour's lo record and nothing
+// of its hi record.
+constexpr int kEntryBits = 24;
+constexpr int kEntryMask = (1 << kEntryBits) - 1;
+__device__ __forceinline__ int type_class(int t) {
+    return t == MAT_FLUID ? 0 : t == MAT_SOIL ? 1 : t == MAT_DUMMY ? 2 : t == MAT_REP ? 3 : 4;
+}
+__device__ __forceinline__ int class_type(int c) {
+    return c == 0 ? MAT_FLUID : c == 1 ? MAT_SOIL : c == 2 ? MAT_DUMMY : c == 3 ? MAT_REP : MAT_RIGID;
+}
+__device__ __forceinline__ int make_entry(int j, int tj, int ox, int oy, int oz) {
+    const unsigned code = (unsigned)((ox + 1) * 9 + (oy + 1) * 3 + (oz + 1));
+    return (int)((unsigned)j | ((unsigned)type_class(tj) << kEntryBits) | (code << 27));
+}
+// Entry for neighbour j of i from their hi records (list builders without staged offsets).
+__device__ __forceinline__ int entry_of(const K32& k, int j, const float4& hi_i, const float4& hi_j) {
+    return make_entry(j, tf_type(hi_j.w), (int)rintf((hi_i.x - hi_j.x) * k.inv_Q),
+                      (int)rintf((hi_i.y - hi_j.y) * k.inv_Q), (int)rintf((hi_i.z - hi_j.z) * k.inv_Q));
+}
+__device__ __forceinline__ int entry_index(const K32&, int e) { return e & kEntryMask; }
 
 // Block-compensated accumulator: plain partial sums, Kahan-folded every flush.
 struct CSum {
@@ -176,7 +203,10 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
 }
 
 // Iterate i's neighbour list (FB = false) or traverse its stencil directly (FB = true: the
-// particle's list overflowed).  The next list index is fetched one iteration ahead.
+// particle's list overflowed).  body(j, d, r2, slot, type_j, m_V_j) gets the exact f32
+// displacement x_i - x_j of every neighbour within the support.  Two neighbours per trip;
+// the next trip's two list entries are loaded before this trip's gathers, so the entry
+// stream (from DRAM) overlaps the gathers and the maths.
 template <int DIM, bool FB, class F>
 __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
                                          const float4* __restrict__ HI, const float4* __restrict__ LO,
@@ -184,41 +214,42 @@ __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restr
                                          const int* __restrict__ sstart, bool flow_i, F&& body) {
     if (!FB) {
         const int m = cnt[i];
-        const float4 hi_i = HI[i], lo_i = LO[i];
+        const float4 lo_i = LO[i];
         const size_t stride = (size_t)k.n;
         const int* lp = nbr + i;
-        // two neighbours per trip; the next trip's two list entries are loaded before this
-        // trip's gathers, so the entry stream (from DRAM) overlaps the gathers and the maths
+        // neighbour record: position difference, type, m_V (lists hold support + skin)
+        auto visit = [&](int e, const float4& l, int s) {
+            const int code = (int)((unsigned)e >> 27);
+            const float ox = (float)(code / 9 - 1), oy = (float)((code / 3) % 3 - 1), oz = (float)(code % 3 - 1);
+            float d[3];
+            d[0] = ox * k.Q + (lo_i.x - l.x);
+            d[1] = oy * k.Q + (lo_i.y - l.y);
+            d[2] = DIM == 3 ? oz * k.Q + (lo_i.z - l.z) : 0.f;
+            float r2 = d[0] * d[0] + d[1] * d[1];
+            if (DIM == 3) r2 += d[2] * d[2];
+            if (r2 < k.R2) body(e & kEntryMask, d, r2, s, class_type((e >> kEntryBits) & 7), l.w);
+        };
         int s = 0;
-        int j0 = 0, j1 = 0;
-        if (m > 1) { j0 = lp[0]; j1 = lp[stride]; lp += 2 * stride; }
+        int e0 = 0, e1 = 0;
+        if (m > 1) { e0 = lp[0]; e1 = lp[stride]; lp += 2 * stride; }
         for (; s + 1 < m; s += 2) {
             int n0 = 0, n1 = 0;
             if (s + 3 < m) { n0 = lp[0]; n1 = lp[stride]; lp += 2 * stride; }
-            const float4 h0 = HI[j0], l0 = LO[j0], h1 = HI[j1], l1 = LO[j1];
-            float d0[3], d1[3];
-            delta<DIM>(hi_i, lo_i, h0, l0, d0);
-            delta<DIM>(hi_i, lo_i, h1, l1, d1);
-            float r20 = d0[0] * d0[0] + d0[1] * d0[1];
-            float r21 = d1[0] * d1[0] + d1[1] * d1[1];
-            if (DIM == 3) { r20 += d0[2] * d0[2]; r21 += d1[2] * d1[2]; }
-            if (r20 < k.R2) body(j0, d0, r20, s);        // lists hold support + skin
-            if (r21 < k.R2) body(j1, d1, r21, s + 1);
-            j0 = n0;
-            j1 = n1;
+            const float4 l0 = LO[e0 & kEntryMask], l1 = LO[e1 & kEntryMask];
+            visit(e0, l0, s);
+            visit(e1, l1, s + 1);
+            e0 = n0;
+            e1 = n1;
         }
         if (s < m) {
-            const int j = nbr[(size_t)s * stride + i];
-            float d[3];
-            delta<DIM>(hi_i, lo_i, HI[j], LO[j], d);
-            float r2 = d[0] * d[0] + d[1] * d[1];
-            if (DIM == 3) r2 += d[2] * d[2];
-            if (r2 < k.R2) body(j, d, r2, s);
+            const int e = nbr[(size_t)s * stride + i];
+            visit(e, LO[e & kEntryMask], s);
         }
     } else {
         int s = 0;
-        enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i,
-                            [&](int j, const float* d, float r2) { body(j, d, r2, s++); });
+        enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float* d, float r2) {
+            body(j, d, r2, s++, tf_type(HI[j].w), LO[j].w);
+        });
     }
 }
 
@@ -244,8 +275,8 @@ struct Ovf {
 
 // Persistent per-particle state of the FP32-mixed form.
 struct P32 {
-    float4* hi;     // (hx, hy, hz, m_V)
-    float4* lo;     // (lx, ly, lz, type word)
+    float4* hi;     // (hx, hy, hz, type word)
+    float4* lo;     // (lx, ly, lz, m_V)
     float4* vel;    // (vx, vy, vz, pressure)
     float* drho;    // density - rho0
     float* mass;
