@@ -1374,7 +1374,7 @@ __global__ void k_offset(int* a, long long m, int off) {
 int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp, bool from_device,
                 Fp32State** out, cudaStream_t s, const Fp32Scenes* scenes) {
     *out = nullptr;
-    if (c.n > (1 << kEntryBits)) return TSG_E_CAPACITY;  // neighbour-list entries index 2^24 particles
+    if (c.n > (1 << kEntryBits)) return TSG_E_CAPACITY;  // neighbour-list entries index 2^23 particles
 
     Fp32State* st = new Fp32State();
     st->c = c;

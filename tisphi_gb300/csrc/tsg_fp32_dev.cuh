@@ -43,14 +43,14 @@ __device__ __forceinline__ int tf_scene(float w) { return (__float_as_int(w) >> 
 constexpr int kMaxScenes = 4096;
 __device__ __forceinline__ bool is_flow(int t) { return t == MAT_FLUID || t == MAT_SOIL; }
 
-// Neighbour-list entries pack the neighbour index (bits 0-23, so this form holds at most
-// 2^24 particles), its material class (bits 24-26: fluid, soil, dummy, repulsive, rigid)
-// and the offset (hi_i - hi_j) / Q of the two particles' quantised positions (bits 27-31:
-// base-3 code of three offsets in -1..1; Q is at least one cell of the list grid, so two
-// listed particles are never more than one quantum apart, and hi only changes when the
-// lists are rebuilt).  A traversal therefore reads the neighbour's lo record and nothing
-// of its hi record.
-constexpr int kEntryBits = 24;
+// Neighbour-list entries pack the neighbour index (bits 0-22, so this form holds at most
+// 2^23 particles), its material class (bits 23-25: fluid, soil, dummy, repulsive, rigid)
+// and the offset (hi_i - hi_j) / Q + 1 of the two particles' quantised positions per axis
+// (bits 26-27, 28-29, 30-31; Q is at least one cell of the list grid, so two listed
+// particles are never more than one quantum apart, and hi only changes when the lists are
+// rebuilt).  A traversal therefore reads the neighbour's lo record and nothing of its hi
+// record, and decodes the entry with shifts and masks.
+constexpr int kEntryBits = 23;
 constexpr int kEntryMask = (1 << kEntryBits) - 1;
 __device__ __forceinline__ int type_class(int t) {
     return t == MAT_FLUID ? 0 : t == MAT_SOIL ? 1 : t == MAT_DUMMY ? 2 : t == MAT_REP ? 3 : 4;
@@ -59,8 +59,11 @@ __device__ __forceinline__ int class_type(int c) {
     return c == 0 ? MAT_FLUID : c == 1 ? MAT_SOIL : c == 2 ? MAT_DUMMY : c == 3 ? MAT_REP : MAT_RIGID;
 }
 __device__ __forceinline__ int make_entry(int j, int tj, int ox, int oy, int oz) {
-    const unsigned code = (unsigned)((ox + 1) * 9 + (oy + 1) * 3 + (oz + 1));
-    return (int)((unsigned)j | ((unsigned)type_class(tj) << kEntryBits) | (code << 27));
+    return (int)((unsigned)j | ((unsigned)type_class(tj) << kEntryBits) | ((unsigned)(ox + 1) << 26) |
+                 ((unsigned)(oy + 1) << 28) | ((unsigned)(oz + 1) << 30));
+}
+__device__ __forceinline__ float entry_offset(int e, int axis) {
+    return (float)((int)(((unsigned)e >> (26 + 2 * axis)) & 3u) - 1);
 }
 // Entry for neighbour j of i from their hi records (list builders without staged offsets).
 __device__ __forceinline__ int entry_of(const K32& k, int j, const float4& hi_i, const float4& hi_j) {
@@ -219,12 +222,10 @@ __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restr
         const int* lp = nbr + i;
         // neighbour record: position difference, type, m_V (lists hold support + skin)
         auto visit = [&](int e, const float4& l, int s) {
-            const int code = (int)((unsigned)e >> 27);
-            const float ox = (float)(code / 9 - 1), oy = (float)((code / 3) % 3 - 1), oz = (float)(code % 3 - 1);
             float d[3];
-            d[0] = ox * k.Q + (lo_i.x - l.x);
-            d[1] = oy * k.Q + (lo_i.y - l.y);
-            d[2] = DIM == 3 ? oz * k.Q + (lo_i.z - l.z) : 0.f;
+            d[0] = entry_offset(e, 0) * k.Q + (lo_i.x - l.x);
+            d[1] = entry_offset(e, 1) * k.Q + (lo_i.y - l.y);
+            d[2] = DIM == 3 ? entry_offset(e, 2) * k.Q + (lo_i.z - l.z) : 0.f;
             float r2 = d[0] * d[0] + d[1] * d[1];
             if (DIM == 3) r2 += d[2] * d[2];
             if (r2 < k.R2) body(e & kEntryMask, d, r2, s, class_type((e >> kEntryBits) & 7), l.w);
