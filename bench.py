@@ -44,10 +44,14 @@ FALLBACK_HBM = 6800.0
 def workload(args):
     from tisphi_gb300 import scenes
     if args.workload == "3d":
-        return scenes.dambreak_3d(spacing=args.spacing), "3D WCSPH dambreak"
-    if args.workload == "2d":
-        return scenes.dambreak_2d(), "2D WCSPH dambreak"
-    raise SystemExit(f"unknown workload {args.workload}")
+        d, name = scenes.dambreak_3d(spacing=args.spacing), "3D WCSPH dambreak"
+    elif args.workload == "2d":
+        d, name = scenes.dambreak_2d(), "2D WCSPH dambreak"
+    else:
+        raise SystemExit(f"unknown workload {args.workload}")
+    if args.list_skin is not None:
+        d["Configuration"]["neighbourSkin"] = args.list_skin
+    return d, name
 
 
 def hbm_peak():
@@ -425,6 +429,7 @@ def run_ours(args):
                                f"{h['n_total'] - h['n_fluid']:,} dummy particles, LF dt 2e-5, CSPM on, XSPH off",
                    "form": head, "n_fluid": h["n_fluid"], "n_total": h["n_total"],
                    "l2": "working set > 129 MB L2 (no flush needed)",
+                   "list_skin": cfg_dict["Configuration"].get("neighbourSkin", 0.05),
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "forms": {k: ({"value": v["value"], "ms_per_step": v["ms_per_step"]} if "value" in v else v)
                   for k, v in forms.items()},
@@ -443,7 +448,7 @@ def run_ours(args):
     }
     if "fp32_mixed" in forms and "fp64" in forms and "value" in forms["fp32_mixed"] and "value" in forms["fp64"]:
         line["speedup_fp32_mixed_vs_fp64"] = forms["fp32_mixed"]["value"] / forms["fp64"]["value"]
-    if rank == 0 and head == "fp32_mixed" and args.workload == "3d":
+    if rank == 0 and head == "fp32_mixed" and args.workload == "3d" and not args.no_full_run:
         line["forms"]["fp32_mixed"]["full_1000_step_run"] = full_run(cfg_dict)
     if rank == 0 and not args.no_errors and all("value" in forms.get(p, {}) for p in ("fp32_mixed", "fp64")):
         line["errors"] = error_report(cfg_dict)
@@ -623,8 +628,11 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=2000, help="rollout length for --workload adjoint")
     ap.add_argument("--scenes", type=int, default=256, help="ensemble size for --workload batch")
     ap.add_argument("--spacing", type=float, default=0.0054)
+    ap.add_argument("--list-skin", type=float, default=None,
+                    help="FP32-mixed neighbour-list skin as a fraction of the support radius (scene default 0.05)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-full-run", action="store_true", help="skip the 1,000-step FP32-mixed run")
     ap.add_argument("--no-errors", action="store_true", help="skip the FP32-mixed vs FP64 error report")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -213,7 +213,7 @@ __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells,
                                     const float dz = rz - q.z;
                                     r2 += dz * dz;
                                 }
-                                const bool ok_type = flow_i || (__float_as_int(q.w) & 7) <= 1;
+                                const bool ok_type = flow_i || is_flow(class_type(__float_as_int(q.w) & 7));
                                 acc |= (t < mm && r2 < k.R2L && ok_type) ? (1u << t) : 0u;
                             }
                             if (i >= base && i < base + 32) acc &= ~(1u << (i - base));
@@ -299,51 +299,61 @@ __global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float
 }
 
 // Inverse of the CSPM matrix (2D: the 2 x 2 block, zero (2, 2) entry; identity when
-// |det| <= 1e-8, eng/solver_sph_base.py:400-423), in f32 like the rest of this form.
+// |det| <= 1e-8, eng/solver_sph_base.py:400-423), in f32 like the rest of this form.  The
+// matrix sum_j m_Vj (-dx_j) (grad W_j)^T is symmetric (grad W is parallel to dx), so it
+// and its inverse are held as six planes (xx, yy, zz, xy, xz, yz); m holds them too.
 template <int DIM>
 __device__ __forceinline__ void inv_store(const K32& k, float* L, int i, const float* m, bool flow_i) {
-    float inv[9] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
+    float inv[6] = {1.f, 1.f, 1.f, 0.f, 0.f, 0.f};
     if (flow_i) {
+        const float xx = m[0], yy = m[1], zz = m[2], xy = m[3], xz = m[4], yz = m[5];
         if (DIM == 2) {
-            const float dt = m[0] * m[4] - m[1] * m[3];
+            const float dt = xx * yy - xy * xy;
             if (fabsf(dt) > (float)EPS) {
                 const float id = 1.f / dt;
-                inv[0] = id * m[4]; inv[1] = -id * m[1]; inv[3] = -id * m[3]; inv[4] = id * m[0]; inv[8] = 0.f;
+                inv[0] = id * yy; inv[1] = id * xx; inv[2] = 0.f; inv[3] = -id * xy;
             }
         } else {
-            const float dt = m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) +
-                             m[6] * (m[1] * m[5] - m[4] * m[2]);
+            const float c00 = yy * zz - yz * yz, c11 = xx * zz - xz * xz, c22 = xx * yy - xy * xy;
+            const float c01 = xz * yz - xy * zz, c02 = xy * yz - yy * xz, c12 = xy * xz - xx * yz;
+            const float dt = xx * c00 + xy * c01 + xz * c02;
             if (fabsf(dt) > (float)EPS) {
                 const float id = 1.f / dt;
-                for (int a = 0; a < 3; ++a)
-                    for (int b = 0; b < 3; ++b)
-                        inv[3 * b + a] = id * (m[3 * ((a + 1) % 3) + (b + 1) % 3] * m[3 * ((a + 2) % 3) + (b + 2) % 3] -
-                                               m[3 * ((a + 2) % 3) + (b + 1) % 3] * m[3 * ((a + 1) % 3) + (b + 2) % 3]);
+                inv[0] = id * c00; inv[1] = id * c11; inv[2] = id * c22;
+                inv[3] = id * c01; inv[4] = id * c02; inv[5] = id * c12;
             }
         }
     }
-    for (int q = 0; q < 9; ++q) L[(size_t)q * k.n + i] = inv[q];
+    for (int q = 0; q < 6; ++q) L[(size_t)q * k.n + i] = inv[q];
+}
+
+// The inverse CSPM matrix of particle i as a full 3 x 3 (row-major) from its six planes.
+__device__ __forceinline__ void load_L(const float* __restrict__ L6, size_t n, int i, float* L) {
+    float l[6];
+    for (int q = 0; q < 6; ++q) l[q] = L6[(size_t)q * n + i];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) L[3 * a + b] = l[sym_idx(a, b)];
 }
 
 // CSPM (eng/solver_sph_base.py:386-423).
 template <int DIM, bool FB>
-__global__ void k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
+__global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                          const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.n, ovf, t.cnt, k.maxn, {
         const int ti = tf_type(p.hi[i].w);
         const bool flow_i = is_flow(ti);
         const bool want_L = k.corr == 1 && flow_i;
         CSum s;
-        float L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        float L[6] = {0, 0, 0, 0, 0, 0};
         for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, flow_i,
                           [&](int j, const float* d, float r2, int sidx, int tj, float mVj) {
-            const float r = fast_sqrt(r2);
-            if (is_flow(tj)) s.add(mVj * w_val(k, r));
+            const WG wg = w_pair<true, true>(k, r2);
+            if (is_flow(tj)) s.add(mVj * wg.w);
             if ((sidx & 7) == 7) s.flush();
             if (want_L && tj == ti) {
-                const float gf = w_grad(k, r) * mVj;
+                const float gf = wg.g * mVj;
                 for (int a = 0; a < DIM; ++a)
-                    for (int b = 0; b < DIM; ++b) L[3 * a + b] += (-d[a]) * (gf * d[b]);
+                    for (int b = a; b < DIM; ++b) L[sym_idx(a, b)] += (-d[a]) * (gf * d[b]);
             }
         });
         const float sum = s.get();
@@ -409,7 +419,7 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
             const float4 hi_i = p.hi[i], lo_i = p.lo[i];
             for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
                               [&](int j, const float* d, float r2, int sidx, int, float mV) {
-                const float w = w_val(k, fast_sqrt(r2));
+                const float w = w_pair<true, false>(k, r2).w;
                 const float4 vt = t.vt[j];
                 const float2 pr = t.pr[j];
                 const float mw = mV * w;
@@ -446,33 +456,34 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         const float visc_b = k.rho0 / rti;
         float L[9];
         if (CORR)
-            for (int q = 0; q < 9; ++q) L[q] = t.L[(size_t)q * k.n + i];
+            load_L(t.L, k.n, i, L);
         CSum dd, dv[3];
         const bool rep_on = k.boundary == 3 || k.boundary == 4;
-        for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
-                          [&](int j, const float* d, float r2, int sidx, int tj, float mVj) {
-            const float4 vtj = t.vt[j];
-            const float r = fast_sqrt(r2);
-            const float gf = w_grad(k, r);
-            const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = vti.z - vtj.z;
-            // continuity: m_Vj (v_i - v_j) . (L_i grad W)
-            const float gx = gf * d[0], gy = gf * d[1], gz = DIM == 3 ? gf * d[2] : 0.f;
-            if (CORR) {
-                const float cx = L[0] * gx + L[1] * gy + (DIM == 3 ? L[2] * gz : 0.f);
-                const float cy = L[3] * gx + L[4] * gy + (DIM == 3 ? L[5] * gz : 0.f);
-                const float cz = DIM == 3 ? L[6] * gx + L[7] * gy + L[8] * gz : 0.f;
-                dd.add(mVj * (dvx * cx + dvy * cy + (DIM == 3 ? dvz * cz : 0.f)));
-            } else {
-                dd.add(mVj * (dvx * gx + dvy * gy + (DIM == 3 ? dvz * gz : 0.f)));
-            }
-            // viscosity (fluid or boundary neighbours) and pressure, on the uncorrected gradient
+        // viscosity factor for fluid and for boundary neighbours; -rho0 p_i / rho_i^2
+        const float vf_f = visc_fac, vf_b = visc_fac * visc_b;
+        const float pi_n = -k.rho0 * vti.w;
+        for_nbrs_g<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
+                            [&](int j) { return __ldg(t.vt + j); },
+                            [&](int, const float* d, float r2, int sidx, int tj, float mVj, const float4& vtj) {
+            const WG wg = w_pair<false, true>(k, r2);
+            const float r = wg.r;
+            const float mg = mVj * wg.g;   // m_Vj G, grad W = G d
+            const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = DIM == 3 ? vti.z - vtj.z : 0.f;
             const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
+            // continuity: m_Vj (v_i - v_j) . (L_i grad W) = m_Vj G (L_i (v_i - v_j)) . d (L_i symmetric)
+            float cdx = vdx;
+            if (CORR) {
+                const float ux = L[0] * dvx + L[1] * dvy + (DIM == 3 ? L[2] * dvz : 0.f);
+                const float uy = L[3] * dvx + L[4] * dvy + (DIM == 3 ? L[5] * dvz : 0.f);
+                const float uz = DIM == 3 ? L[6] * dvx + L[7] * dvy + L[8] * dvz : 0.f;
+                cdx = ux * d[0] + uy * d[1] + (DIM == 3 ? uz * d[2] : 0.f);
+            }
+            dd.add(mg * cdx);
+            // viscosity (fluid or boundary neighbours) and pressure, on the uncorrected gradient.
             // WCSPH scenes hold fluid, dummy, repulsive and rigid particles only (soil is rejected
             // at upload), so every non-fluid neighbour takes the boundary form
-            const float cv = __fdividef(visc_fac * mVj * fminf(vdx, 0.f), r2 + k.eps_h2) *
-                             (tj == MAT_FLUID ? 1.f : visc_b);
-            const float cp = -k.rho0 * mVj * (vti.w + vtj.w);
-            float sc = (cv + cp) * gf;
+            const float cv = (tj == MAT_FLUID ? vf_f : vf_b) * __fdividef(fminf(vdx, 0.f), r2 + k.eps_h2);
+            float sc = mg * (cv + fmaf(-k.rho0, vtj.w, pi_n));
             float rs = 0.f;
             if (rep_on && tj == MAT_REP) {  // repulsive force (eng/solver_sph_base.py:675-689)
                 const float chi = (r > 0.f && r < k.diam) ? 1.f - r / k.diam : 0.f;
@@ -517,7 +528,7 @@ __global__ void k_mui_stress32(K32 k, P32 p, T32 t, const float4* __restrict__ P
         const float4 vti = t.vt[i], vli = t.vtlo[i];
         float L[9];
         if (CORR)
-            for (int q = 0; q < 9; ++q) L[q] = t.L[(size_t)q * k.n + i];
+            load_L(t.L, k.n, i, L);
         float vg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         CSum dd;
         for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
@@ -595,7 +606,7 @@ __global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
         const float4 vti = t.vt[i], vli = t.vtlo[i];
         float L[9];
         if (CORR)
-            for (int q = 0; q < 9; ++q) L[q] = t.L[(size_t)q * n + i];
+            load_L(t.L, n, i, L);
         float sti[6];
         load_sym(t.sigt, n, i, sti);
         const float rti = k.rho0 + t.drt[i];
@@ -1019,7 +1030,12 @@ __global__ void k_export(K32 k, P32 p, T32 t, int what, double* out, size_t sq, 
     case 8: o[0] = t.dd[i]; break;
     case 9: { float4 v = t.dv[i]; o[0] = v.x; o[sq] = v.y; o[2 * sq] = v.z; break; }
     case 10: o[0] = t.cf[i]; break;
-    case 11: for (int q = 0; q < 9; ++q) o[q * sq] = t.L ? t.L[(size_t)q * n + i] : 0.0; break;
+    case 11: {  // CSPM_L: full 3 x 3 from the six stored planes
+        float L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (t.L) load_L(t.L, n, i, L);
+        for (int q = 0; q < 9; ++q) o[q * sq] = L[q];
+        break;
+    }
     case 12: case 13: case 14: {  // stress, stress_tmp, d_stress: full 3 x 3 from the six stored
         const float* a = what == 12 ? p.sig : what == 13 ? t.sigt : t.dsig;
         for (int r = 0; r < 3; ++r)
@@ -1395,6 +1411,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     k.wgrad = (float)(-5.0 * c.kk * c.h1 * c.h1);
     k.cub1 = (float)(c.kk * c.h1);
     k.cub2 = (float)(-0.5 * c.kk * c.h1);
+    k.cub1h = (float)(c.kk * c.h1 * c.h1);
     k.R2 = (float)(c.R * c.R);
     k.R2hi = std::nextafter((float)(c.R * c.R * (1.0 + 1.0 / 1024.0)), 1e30f);
     k.R2lo = (float)(c.R * c.R * (1.0 - 1.0 / 1024.0));
@@ -1454,7 +1471,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     T32& t = st->T;
     t.vt = dal<float4>(*st, n); t.pr = dal<float2>(*st, n); t.drt = dal<float>(*st, n); t.dd = dal<float>(*st, n);
     t.dv = dal<float4>(*st, n); t.cf = dal<float>(*st, n); t.xs = dal<float4>(*st, n);
-    t.L = c.corr == 1 ? dal<float>(*st, 9 * (size_t)n) : nullptr;
+    t.L = c.corr == 1 ? dal<float>(*st, 6 * (size_t)n) : nullptr;
     t.cnt = dal<int>(*st, n);
     t.nbr = dal<int>(*st, (size_t)k.maxn * n);
     if (c.ti == 4) {

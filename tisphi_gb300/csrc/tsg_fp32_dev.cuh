@@ -22,7 +22,7 @@ struct K32 {
     int gnum[3];
     long long G;
     double vs[3], grid;
-    float Q, inv_grid, h1, kk, kk6, wgrad, cub1, cub2, R2, R2lo, R2hi, pf_lim;
+    float Q, inv_grid, h1, kk, kk6, wgrad, cub1, cub2, cub1h, R2, R2lo, R2hi, pf_lim;
     float R2L, R2Lhi, disp2_limit;  // list radius (support + skin) and rebuild threshold
     float visc_fac, eps_h2, rho0, B, gamma, dt, hdt, dt6, g[3], rep_fac, diam, h075, r_eps;
     float ds[3], de[3];
@@ -44,26 +44,25 @@ constexpr int kMaxScenes = 4096;
 __device__ __forceinline__ bool is_flow(int t) { return t == MAT_FLUID || t == MAT_SOIL; }
 
 // Neighbour-list entries pack the neighbour index (bits 0-22, so this form holds at most
-// 2^23 particles), its material class (bits 23-25: fluid, soil, dummy, repulsive, rigid)
-// and the offset (hi_i - hi_j) / Q + 1 of the two particles' quantised positions per axis
-// (bits 26-27, 28-29, 30-31; Q is at least one cell of the list grid, so two listed
-// particles are never more than one quantum apart, and hi only changes when the lists are
-// rebuilt).  A traversal therefore reads the neighbour's lo record and nothing of its hi
-// record, and decodes the entry with shifts and masks.
+// 2^23 particles), its material type (bits 23-25: type + 2 for repulsive, dummy, fluid and
+// soil, 7 for rigid) and the offset (hi_i - hi_j) / Q + 1 of the two particles' quantised
+// positions per axis (bits 26-27, 28-29, 30-31; Q is at least one cell of the list grid,
+// so two listed particles are never more than one quantum apart, and hi only changes when
+// the lists are rebuilt).  A traversal therefore reads the neighbour's lo record and
+// nothing of its hi record, and decodes the entry with shifts, masks and one float add per
+// axis.
 constexpr int kEntryBits = 23;
 constexpr int kEntryMask = (1 << kEntryBits) - 1;
-__device__ __forceinline__ int type_class(int t) {
-    return t == MAT_FLUID ? 0 : t == MAT_SOIL ? 1 : t == MAT_DUMMY ? 2 : t == MAT_REP ? 3 : 4;
-}
-__device__ __forceinline__ int class_type(int c) {
-    return c == 0 ? MAT_FLUID : c == 1 ? MAT_SOIL : c == 2 ? MAT_DUMMY : c == 3 ? MAT_REP : MAT_RIGID;
-}
+__device__ __forceinline__ int type_class(int t) { return t == MAT_RIGID ? 7 : t + 2; }
+__device__ __forceinline__ int class_type(int c) { return c == 7 ? MAT_RIGID : c - 2; }
 __device__ __forceinline__ int make_entry(int j, int tj, int ox, int oy, int oz) {
     return (int)((unsigned)j | ((unsigned)type_class(tj) << kEntryBits) | ((unsigned)(ox + 1) << 26) |
                  ((unsigned)(oy + 1) << 28) | ((unsigned)(oz + 1) << 30));
 }
+// Offset field v of an axis as the float v - 1: v in the low mantissa bits of 2^23 gives
+// the float 2^23 + v exactly, and subtracting 2^23 + 1 is exact.
 __device__ __forceinline__ float entry_offset(int e, int axis) {
-    return (float)((int)(((unsigned)e >> (26 + 2 * axis)) & 3u) - 1);
+    return __int_as_float((int)(0x4B000000u | (((unsigned)e >> (26 + 2 * axis)) & 3u))) - 8388609.f;
 }
 // Entry for neighbour j of i from their hi records (list builders without staged offsets).
 __device__ __forceinline__ int entry_of(const K32& k, int j, const float4& hi_i, const float4& hi_j) {
@@ -139,6 +138,36 @@ __device__ __forceinline__ float w_grad(const K32& k, float r) {
     return k.cub2 * f * f * inv;                       // -0.5 k h1 f^2 / r
 }
 
+// Kernel value and gradient factor of a neighbour at squared distance r2 (within the
+// support), from one reciprocal square root rs = 1 / r: the cubic spline's inner piece
+// k h^-1 q (1.5 q - 2) / r is k h^-2 (1.5 q - 2) (q / r = 1 / h), the outer piece takes
+// 1 / r from rs.  r = 0 gives r = NaN and both factors 0.
+struct WG { float r, w, g; };
+template <bool VAL, bool GRAD>
+__device__ __forceinline__ WG w_pair(const K32& k, float r2) {
+    const float rs = rsqrtf(r2);
+    WG o;
+    o.r = r2 * rs;
+    o.w = 0.f;
+    o.g = 0.f;
+    const float q = o.r * k.h1;
+    if (!(o.r > 1e-8f && q <= 2.f)) return o;
+    if (k.kernel == 1) {
+        const float q1 = 1.f - 0.5f * q, q2 = q1 * q1;
+        if (VAL) o.w = k.kk * (q2 * q2) * (1.f + 2.f * q);
+        if (GRAD) o.g = k.wgrad * (q2 * q1);
+        return o;
+    }
+    const float t = 2.f - q;
+    if (q <= 1.f) {
+        if (VAL) o.w = k.kk * ((0.5f * q - 1.f) * q * q + 2.f / 3.f);
+        if (GRAD) o.g = k.cub1h * (1.5f * q - 2.f);
+    } else {
+        if (VAL) o.w = k.kk6 * t * t * t;
+        if (GRAD) o.g = k.cub2 * t * t * rs;
+    }
+    return o;
+}
 template <int DIM>
 __device__ __forceinline__ void delta(const float4& hi_i, const float4& lo_i, const float4& hi_j, const float4& lo_j,
                                       float* d) {
@@ -206,29 +235,31 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
 }
 
 // Iterate i's neighbour list (FB = false) or traverse its stencil directly (FB = true: the
-// particle's list overflowed).  body(j, d, r2, slot, type_j, m_V_j) gets the exact f32
-// displacement x_i - x_j of every neighbour within the support.  Two neighbours per trip;
+// particle's list overflowed).  body(j, d, r2, slot, type_j, m_V_j, g_j) gets the exact f32
+// displacement x_i - x_j of every neighbour within the support and g_j = gather(j), the
+// neighbour's payload, loaded together with its lo record (before the support test, so the
+// two gathers overlap; the list's skin pairs load it for nothing).  Two neighbours per trip;
 // the next trip's two list entries are loaded before this trip's gathers, so the entry
 // stream (from DRAM) overlaps the gathers and the maths.
-template <int DIM, bool FB, class F>
-__device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
-                                         const float4* __restrict__ HI, const float4* __restrict__ LO,
-                                         const float4* __restrict__ PF, const int* __restrict__ dstart,
-                                         const int* __restrict__ sstart, bool flow_i, F&& body) {
+template <int DIM, bool FB, class G, class F>
+__device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
+                                           const float4* __restrict__ HI, const float4* __restrict__ LO,
+                                           const float4* __restrict__ PF, const int* __restrict__ dstart,
+                                           const int* __restrict__ sstart, bool flow_i, G&& gather, F&& body) {
     if (!FB) {
         const int m = cnt[i];
         const float4 lo_i = LO[i];
         const size_t stride = (size_t)k.n;
         const int* lp = nbr + i;
         // neighbour record: position difference, type, m_V (lists hold support + skin)
-        auto visit = [&](int e, const float4& l, int s) {
+        auto visit = [&](int e, const float4& l, const auto& g, int s) {
             float d[3];
             d[0] = entry_offset(e, 0) * k.Q + (lo_i.x - l.x);
             d[1] = entry_offset(e, 1) * k.Q + (lo_i.y - l.y);
             d[2] = DIM == 3 ? entry_offset(e, 2) * k.Q + (lo_i.z - l.z) : 0.f;
             float r2 = d[0] * d[0] + d[1] * d[1];
             if (DIM == 3) r2 += d[2] * d[2];
-            if (r2 < k.R2) body(e & kEntryMask, d, r2, s, class_type((e >> kEntryBits) & 7), l.w);
+            if (r2 < k.R2) body(e & kEntryMask, d, r2, s, class_type((e >> kEntryBits) & 7), l.w, g);
         };
         int s = 0;
         int e0 = 0, e1 = 0;
@@ -236,22 +267,42 @@ __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restr
         for (; s + 1 < m; s += 2) {
             int n0 = 0, n1 = 0;
             if (s + 3 < m) { n0 = lp[0]; n1 = lp[stride]; lp += 2 * stride; }
-            const float4 l0 = LO[e0 & kEntryMask], l1 = LO[e1 & kEntryMask];
-            visit(e0, l0, s);
-            visit(e1, l1, s + 1);
+            const int j0 = e0 & kEntryMask, j1 = e1 & kEntryMask;
+            const float4 l0 = LO[j0], l1 = LO[j1];
+            const auto g0 = gather(j0);
+            const auto g1 = gather(j1);
+            // s is even: the slot numbers' low bit is known, so a body's test of the slot
+            // (a flush every eight) is decided at compile time for the first of the pair
+            visit(e0, l0, g0, s & ~1);
+            visit(e1, l1, g1, s | 1);
             e0 = n0;
             e1 = n1;
         }
         if (s < m) {
             const int e = nbr[(size_t)s * stride + i];
-            visit(e, LO[e & kEntryMask], s);
+            const int j = e & kEntryMask;
+            visit(e, LO[j], gather(j), s);
         }
     } else {
         int s = 0;
         enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float* d, float r2) {
-            body(j, d, r2, s++, tf_type(HI[j].w), LO[j].w);
+            body(j, d, r2, s++, tf_type(HI[j].w), LO[j].w, gather(j));
         });
     }
+}
+
+struct NoPayload {};
+
+// for_nbrs_g without a payload: body(j, d, r2, slot, type_j, m_V_j).
+template <int DIM, bool FB, class F>
+__device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
+                                         const float4* __restrict__ HI, const float4* __restrict__ LO,
+                                         const float4* __restrict__ PF, const int* __restrict__ dstart,
+                                         const int* __restrict__ sstart, bool flow_i, F&& body) {
+    for_nbrs_g<DIM, FB>(k, i, cnt, nbr, HI, LO, PF, dstart, sstart, flow_i, [](int) { return NoPayload{}; },
+                        [&](int j, const float* d, float r2, int s, int tj, float mV, NoPayload) {
+                            body(j, d, r2, s, tj, mV);
+                        });
 }
 
 // Particle loop shared by the list kernels (FB = false: one particle per thread, skipping
@@ -301,7 +352,7 @@ struct T32 {
     float* dd;      // d_density
     float4* dv;     // d_vel
     float* cf;      // CSPM_f
-    float* L;       // CSPM_L, 9 planes
+    float* L;       // inverse CSPM matrix, 6 symmetric planes (xx, yy, zz, xy, xz, yz)
     float4* xs;     // XSPH sums
     int* cnt;
     int* nbr;

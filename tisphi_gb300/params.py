@@ -81,7 +81,7 @@ def native_config(cfg, geom, precision="fp64") -> nat.tsg_config:
     c.density0 = mat["density0"]
     c.damping_eps = 5e-5
     # FP32-mixed neighbour-list skin (fraction of the support radius); extension key
-    c.list_skin = float(cfg.get_cfg_opt("neighbourSkin", 0.1))
+    c.list_skin = float(cfg.get_cfg_opt("neighbourSkin", 0.05))
     if mat["matType"] == MAT_FLUID:
         c.viscosity = mat["viscosity"]
         c.stiffness = mat["stiffness"]
