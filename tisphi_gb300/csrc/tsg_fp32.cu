@@ -336,7 +336,7 @@ __device__ __forceinline__ void load_L(const float* __restrict__ L6, size_t n, i
 }
 
 // CSPM (eng/solver_sph_base.py:386-423).
-template <int DIM, bool FB>
+template <int DIM, bool FB, int KT>
 __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                          const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.n, ovf, t.cnt, k.maxn, {
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const fl
         float L[6] = {0, 0, 0, 0, 0, 0};
         for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, flow_i,
                           [&](int j, const float* d, float r2, int sidx, int tj, float mVj) {
-            const WG wg = w_pair<true, true>(k, r2);
+            const WG wg = w_pair<true, true, KT>(k, r2);
             if (is_flow(tj)) s.add(mVj * wg.w);
             if ((sidx & 7) == 7) s.flush();
             if (want_L && tj == ti) {
@@ -408,7 +408,7 @@ __global__ void k_pre32(K32 k, P32 p, T32 t) {
 }
 
 // Boundary extrapolation for dummy / repulsive / rigid particles in [base, base + count_n) (WC).
-template <int DIM, bool FB>
+template <int DIM, bool FB, int KT>
 __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                         const int* __restrict__ sstart, int base, int count_n, Ovf ovf) {
     const int lim = base + count_n;
@@ -419,7 +419,7 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
             const float4 hi_i = p.hi[i], lo_i = p.lo[i];
             for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
                               [&](int j, const float* d, float r2, int sidx, int, float mV) {
-                const float w = w_pair<true, false>(k, r2).w;
+                const float w = w_pair<true, false, KT>(k, r2).w;
                 const float4 vt = t.vt[j];
                 const float2 pr = t.pr[j];
                 const float mw = mV * w;
@@ -444,7 +444,9 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
 }
 
 // WCSPH continuity + momentum (eng/solver_sph_wc.py:108-126).
-template <int DIM, bool FB, bool CORR>
+// KT: kernel function (w_pair); REP: repulsive boundary forces on (1), off (0) or chosen at
+// run time from k.boundary (-1).
+template <int DIM, bool FB, bool CORR, int KT, int REP>
 __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                           const int* __restrict__ sstart, Ovf ovf) {
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
@@ -458,14 +460,14 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         if (CORR)
             load_L(t.L, k.n, i, L);
         CSum dd, dv[3];
-        const bool rep_on = k.boundary == 3 || k.boundary == 4;
+        const bool rep_on = REP < 0 ? (k.boundary == 3 || k.boundary == 4) : REP == 1;
         // viscosity factor for fluid and for boundary neighbours; -rho0 p_i / rho_i^2
         const float vf_f = visc_fac, vf_b = visc_fac * visc_b;
         const float pi_n = -k.rho0 * vti.w;
         for_nbrs_g<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
                             [&](int j) { return __ldg(t.vt + j); },
                             [&](int, const float* d, float r2, int sidx, int tj, float mVj, const float4& vtj) {
-            const WG wg = w_pair<false, true>(k, r2);
+            const WG wg = w_pair<false, true, KT>(k, r2);
             const float r = wg.r;
             const float mg = mVj * wg.g;   // m_Vj G, grad W = G d
             const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = DIM == 3 ? vti.z - vtj.z : 0.f;
@@ -1719,17 +1721,53 @@ bool fp32_rebuild_due(Fp32State& st, cudaStream_t s) {
     return !(d2 <= k.disp2_limit);
 }
 
+// The list kernels' main pass is compiled per kernel function (and, for the rates, per
+// repulsive-boundary mode); their overflow pass (a few particles) decides both at run time.
+template <int DIM>
+void corr_launch(Fp32State& st, cudaStream_t s, const Ovf& ovf) {
+    const K32& k = st.k;
+    const P32& p = st.P[st.cur];
+    const int nb = nblk(k.n, st.tpb);
+    if (k.kernel == 1) TSG_LAUNCH((k_corr32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+    else TSG_LAUNCH((k_corr32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+    TSG_LAUNCH((k_corr32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+}
+
+template <int DIM>
+void bdy_launch(Fp32State& st, const P32& p, int base, int count_n, cudaStream_t s, const Ovf& ovf) {
+    const K32& k = st.k;
+    const int nb = nblk(count_n, st.tpb);
+    if (k.kernel == 1)
+        TSG_LAUNCH((k_bdy32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+    else
+        TSG_LAUNCH((k_bdy32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+    TSG_LAUNCH((k_bdy32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+}
+
+template <int DIM, bool CORR, int KT>
+void rates_main(Fp32State& st, const P32& p, cudaStream_t s, const Ovf& ovf) {
+    const K32& k = st.k;
+    const int nb = nblk(k.nd, st.tpb);
+    if (k.boundary == 3 || k.boundary == 4)
+        TSG_LAUNCH((k_rates32<DIM, false, CORR, KT, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+    else
+        TSG_LAUNCH((k_rates32<DIM, false, CORR, KT, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+}
+
+template <int DIM, bool CORR>
+void rates_launch(Fp32State& st, const P32& p, cudaStream_t s, const Ovf& ovf) {
+    const K32& k = st.k;
+    if (k.kernel == 1) rates_main<DIM, CORR, 1>(st, p, s, ovf);
+    else rates_main<DIM, CORR, 0>(st, p, s, ovf);
+    TSG_LAUNCH((k_rates32<DIM, true, CORR, -1, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+}
+
 void fp32_kernel_corr(Fp32State& st, cudaStream_t s) {
     PhaseScope ph(s, PH_CORR);
     const K32& k = st.k;
     const Ovf ovf{st.ovf_list, st.novf};
-    if (k.dim == 2) {
-        TSG_LAUNCH((k_corr32<2, false>), nblk(k.n, st.tpb), st.tpb, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
-        TSG_LAUNCH((k_corr32<2, true>), 64, TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
-    } else {
-        TSG_LAUNCH((k_corr32<3, false>), nblk(k.n, st.tpb), st.tpb, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
-        TSG_LAUNCH((k_corr32<3, true>), 64, TPB, s, k, st.P[st.cur], st.T, st.pf, st.dstart, st.sstart, ovf);
-    }
+    if (k.dim == 2) corr_launch<2>(st, s, ovf);
+    else corr_launch<3>(st, s, ovf);
 }
 
 void fp32_init_tmp(Fp32State& st, cudaStream_t s) {
@@ -1795,13 +1833,8 @@ void fp32_one_step(Fp32State& st, cudaStream_t s) {
         const Ovf ovf{st.ovf_list, st.novf};
         auto bdy = [&](int base, int count_n) {
             if (count_n <= 0) return;
-            if (k.dim == 2) {
-                TSG_LAUNCH((k_bdy32<2, false>), nblk(count_n, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
-                TSG_LAUNCH((k_bdy32<2, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
-            } else {
-                TSG_LAUNCH((k_bdy32<3, false>), nblk(count_n, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
-                TSG_LAUNCH((k_bdy32<3, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
-            }
+            if (k.dim == 2) bdy_launch<2>(st, p, base, count_n, s, ovf);
+            else bdy_launch<3>(st, p, base, count_n, s, ovf);
         };
         bdy(k.nd, k.n - k.nd);
         if (st.c.n_bdy > k.n - k.nd) bdy(0, k.nd);  // kinematic rigid particles live in the dynamic block
@@ -1809,18 +1842,8 @@ void fp32_one_step(Fp32State& st, cudaStream_t s) {
     {
         PhaseScope ph(s, PH_RATES);
         const Ovf ovf{st.ovf_list, st.novf};
-        const int nb = nblk(k.nd, st.tpb);
-        if (k.dim == 2) {
-            if (k.corr) { TSG_LAUNCH((k_rates32<2, false, true>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-                          TSG_LAUNCH((k_rates32<2, true, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
-            else { TSG_LAUNCH((k_rates32<2, false, false>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-                   TSG_LAUNCH((k_rates32<2, true, false>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
-        } else {
-            if (k.corr) { TSG_LAUNCH((k_rates32<3, false, true>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-                          TSG_LAUNCH((k_rates32<3, true, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
-            else { TSG_LAUNCH((k_rates32<3, false, false>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-                   TSG_LAUNCH((k_rates32<3, true, false>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); }
-        }
+        if (k.dim == 2) { if (k.corr) rates_launch<2, true>(st, p, s, ovf); else rates_launch<2, false>(st, p, s, ovf); }
+        else { if (k.corr) rates_launch<3, true>(st, p, s, ovf); else rates_launch<3, false>(st, p, s, ovf); }
     }
 }
 

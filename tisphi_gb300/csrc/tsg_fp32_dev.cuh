@@ -138,21 +138,24 @@ __device__ __forceinline__ float w_grad(const K32& k, float r) {
     return k.cub2 * f * f * inv;                       // -0.5 k h1 f^2 / r
 }
 
-// Kernel value and gradient factor of a neighbour at squared distance r2 (within the
-// support), from one reciprocal square root rs = 1 / r: the cubic spline's inner piece
-// k h^-1 q (1.5 q - 2) / r is k h^-2 (1.5 q - 2) (q / r = 1 / h), the outer piece takes
-// 1 / r from rs.  r = 0 gives r = NaN and both factors 0.
+// Kernel value and gradient factor of a neighbour at squared distance r2 < R^2, from one
+// reciprocal square root rs = 1 / r: the cubic spline's inner piece k h^-1 q (1.5 q - 2) / r
+// is k h^-2 (1.5 q - 2) (q / r = 1 / h), the outer piece takes 1 / r from rs.  r2 < R^2
+// bounds q = r / h by 2 up to the roundings of r and q, and both kernels vanish at q = 2, so
+// the support test is not repeated here.  r = 0 gives r = NaN and both factors 0.
+// KT selects the kernel function at compile time (1 Wendland C2, 0 cubic spline) or, for
+// -1, at run time from k.kernel.
 struct WG { float r, w, g; };
-template <bool VAL, bool GRAD>
+template <bool VAL, bool GRAD, int KT = -1>
 __device__ __forceinline__ WG w_pair(const K32& k, float r2) {
     const float rs = rsqrtf(r2);
     WG o;
     o.r = r2 * rs;
     o.w = 0.f;
     o.g = 0.f;
+    if (!(o.r > 1e-8f)) return o;
     const float q = o.r * k.h1;
-    if (!(o.r > 1e-8f && q <= 2.f)) return o;
-    if (k.kernel == 1) {
+    if (KT == 1 || (KT < 0 && k.kernel == 1)) {
         const float q1 = 1.f - 0.5f * q, q2 = q1 * q1;
         if (VAL) o.w = k.kk * (q2 * q2) * (1.f + 2.f * q);
         if (GRAD) o.g = k.wgrad * (q2 * q1);
