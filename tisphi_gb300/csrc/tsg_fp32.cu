@@ -337,9 +337,12 @@ __device__ __forceinline__ void load_L(const float* __restrict__ L6, size_t n, i
 
 // CSPM (eng/solver_sph_base.py:386-423).
 template <int DIM, bool FB, int KT>
+// Main pass: the dynamic block, then the static-block particles with a non-empty list
+// (act[0 .. *nact)); the others keep the values written at the list build.
 __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
-                         const int* __restrict__ sstart, Ovf ovf) {
-    FOR_PARTICLES(FB, 0, k.n, ovf, t.cnt, k.maxn, {
+                         const int* __restrict__ sstart, const int* __restrict__ act, const int* __restrict__ nact,
+                         Ovf ovf) {
+    FOR_PARTICLES_ACT(FB, 0, k.nd, act, nact, k.n, ovf, t.cnt, k.maxn, {
         const int ti = tf_type(p.hi[i].w);
         const bool flow_i = is_flow(ti);
         const bool want_L = k.corr == 1 && flow_i;
@@ -410,9 +413,11 @@ __global__ void k_pre32(K32 k, P32 p, T32 t) {
 // Boundary extrapolation for dummy / repulsive / rigid particles in [base, base + count_n) (WC).
 template <int DIM, bool FB, int KT>
 __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
-                        const int* __restrict__ sstart, int base, int count_n, Ovf ovf) {
+                        const int* __restrict__ sstart, int base, int count_n, const int* __restrict__ act,
+                        const int* __restrict__ nact, Ovf ovf) {
     const int lim = base + count_n;
-    FOR_PARTICLES(FB, base, lim, ovf, t.cnt, k.maxn, {
+    // with act: the listed particles of [base, lim) (the main pass's direct range is empty)
+    FOR_PARTICLES_ACT(FB, base, act ? base : lim, act, nact, lim, ovf, t.cnt, k.maxn, {
         const int ti = tf_type(p.hi[i].w);
         if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
             CSum bv[3], bp;
@@ -1494,6 +1499,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     st->tiles = dal<int>(*st, nb / 2048 + 4); st->err = dal<int>(*st, 1);
     st->cells_d = dal<int>(*st, nb); st->cells_s = dal<int>(*st, nb); st->ncells = dal<int>(*st, 2);
     st->ovf_list = dal<int>(*st, n); st->novf = dal<int>(*st, 1);
+    st->sact = dal<int>(*st, n - nd > 0 ? n - nd : 1); st->nsact = dal<int>(*st, 1);
     st->maxdisp = dal<unsigned>(*st, 1);
     st->d_rebuilds = dal<int>(*st, 1);
     st->cells_per_cta = c.dim == 3 ? 4 : 0;
@@ -1643,6 +1649,42 @@ void build_lists(Fp32State& st, const P32& p, cudaStream_t s) {
                st.ovf_list, st.novf);
 }
 
+// Static-block particles (fixed boundary) with a non-empty neighbour list, in warp-sized
+// runs of the block's order (a run's place in the list depends on scheduling; every consumer
+// treats its particles independently, so results do not).  A boundary particle with an
+// empty list has no flow particle within support + skin: no flow particle reads its
+// extrapolated state, and the values of the list kernels for it (Shepard factor 1, identity
+// CSPM matrix, WCSPH extrapolation 2 v with zero pressure) depend on nothing but its own
+// constant velocity; they are written here, once per list build, and the per-step kernels
+// visit the listed particles only.
+__global__ void k_static_active(K32 k, P32 p, T32 t, int wc, int* __restrict__ act, int* __restrict__ nact) {
+    const int i = k.nd + blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = i < k.n;
+    const bool on = in && t.cnt[i] != 0;
+    const unsigned ball = __ballot_sync(0xffffffffu, on);
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0 && ball) base = atomicAdd(nact, __popc(ball));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (on) act[base + __popc(ball & ((1u << lane) - 1u))] = i;
+    if (!in || on) return;
+    t.cf[i] = 1.f;
+    if (t.L) {
+        const size_t n = k.n;
+        for (int q = 0; q < 6; ++q) t.L[q * n + i] = q < 3 ? 1.f : 0.f;
+    }
+    if (!wc) return;
+    const int ti = tf_type(p.hi[i].w);
+    if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
+        const float4 v = p.vel[i];
+        t.vt[i] = make_float4(2.f * v.x, 2.f * v.y, 2.f * v.z, 0.f);
+        t.pr[i] = make_float2(0.f, k.rho0);
+        t.drt[i] = 0.f;
+        p.vel[i].w = 0.f;
+        if (ti == MAT_RIGID) { t.dd[i] = 0.f; t.dv[i] = make_float4(0.f, 0.f, 0.f, 0.f); }
+    }
+}
+
 // Copy the dynamic block of b back into a (graph mode keeps one current buffer).
 __global__ void k_copy_back32(int nd, P32 b, P32 a, size_t n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1664,6 +1706,14 @@ __global__ void k_copy_back32(int nd, P32 b, P32 a, size_t n) {
 
 }  // namespace
 
+// List the static-block particles with a non-empty list and write the state of the others.
+static void static_active(Fp32State& st, cudaStream_t s) {
+    cudaMemsetAsync(st.nsact, 0, sizeof(int), s);
+    if (st.n > st.nd)
+        TSG_LAUNCH(k_static_active, nblk(st.n - st.nd), TPB, s, st.k, st.P[st.cur], st.T, st.k.solver == 1 ? 1 : 0,
+                   st.sact, st.nsact);
+}
+
 // Re-sort the dynamic block and rebuild every list.  in_place keeps the current buffer
 // (the sorted block is copied back), as a captured graph needs fixed pointers.
 void f32::rebuild(Fp32State& st, cudaStream_t s, bool in_place) {
@@ -1681,6 +1731,7 @@ void f32::rebuild(Fp32State& st, cudaStream_t s, bool in_place) {
         PhaseScope ph2(s, PH_LISTS);
         if (st.k.dim == 3) build_lists<3>(st, st.P[st.cur], s);
         else build_lists<2>(st, st.P[st.cur], s);
+        static_active(st, s);
     }
     cudaMemsetAsync(st.maxdisp, 0, sizeof(unsigned), s);
 }
@@ -1723,25 +1774,35 @@ bool fp32_rebuild_due(Fp32State& st, cudaStream_t s) {
 
 // The list kernels' main pass is compiled per kernel function (and, for the rates, per
 // repulsive-boundary mode); their overflow pass (a few particles) decides both at run time.
+// Grids of the main passes cover the largest possible count of listed static particles;
+// the threads past the device count return at once.
 template <int DIM>
 void corr_launch(Fp32State& st, cudaStream_t s, const Ovf& ovf) {
     const K32& k = st.k;
     const P32& p = st.P[st.cur];
     const int nb = nblk(k.n, st.tpb);
-    if (k.kernel == 1) TSG_LAUNCH((k_corr32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-    else TSG_LAUNCH((k_corr32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-    TSG_LAUNCH((k_corr32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+    if (k.kernel == 1)
+        TSG_LAUNCH((k_corr32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact, ovf);
+    else
+        TSG_LAUNCH((k_corr32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact, ovf);
+    TSG_LAUNCH((k_corr32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact, ovf);
 }
 
+// WCSPH boundary extrapolation over [base, base + count_n); the static block (base = nd)
+// visits its listed particles only.
 template <int DIM>
 void bdy_launch(Fp32State& st, const P32& p, int base, int count_n, cudaStream_t s, const Ovf& ovf) {
     const K32& k = st.k;
     const int nb = nblk(count_n, st.tpb);
+    const int* act = base == k.nd ? st.sact : nullptr;
     if (k.kernel == 1)
-        TSG_LAUNCH((k_bdy32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+        TSG_LAUNCH((k_bdy32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, act,
+                   st.nsact, ovf);
     else
-        TSG_LAUNCH((k_bdy32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
-    TSG_LAUNCH((k_bdy32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, ovf);
+        TSG_LAUNCH((k_bdy32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, act,
+                   st.nsact, ovf);
+    TSG_LAUNCH((k_bdy32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, act,
+               st.nsact, ovf);
 }
 
 template <int DIM, bool CORR, int KT>
@@ -2319,6 +2380,9 @@ int fp32_write(Fp32State& st, const char* name, const void* src, bool from_devic
     cudaMemcpyAsync(buf, src, sizeof(double) * comps * n, from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
     TSG_LAUNCH(k_import, nblk(n), TPB, s, st.k, st.P[st.cur], what, buf);
     if (what == 0) st.lists_valid = false;
+    // boundary particles without flow neighbours: their extrapolated state follows the
+    // imported velocity / pressure at once (it is otherwise written at list builds only)
+    if (st.built) static_active(st, s);
     return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
 }
 

@@ -328,6 +328,28 @@ struct Ovf {
         }                                                                                       \
     } while (0)
 
+// FOR_PARTICLES over the direct range [BASE, LIM) followed by the listed particles
+// ACT[0 .. *NACT) (ACT may be null) in the main pass; the overflow pass (FB) takes the
+// overflowed particles in [BASE, N), as FOR_PARTICLES does.
+#define FOR_PARTICLES_ACT(FB, BASE, LIM, ACT, NACT, N, OVF, CNT, MAXN, ...)                     \
+    do {                                                                                        \
+        if (!(FB)) {                                                                            \
+            const int q_ = blockIdx.x * blockDim.x + threadIdx.x;                               \
+            const int nlim_ = (LIM) - (BASE);                                                   \
+            int i_ = -1;                                                                        \
+            if (q_ < nlim_) i_ = (BASE) + q_;                                                   \
+            else if ((ACT) && q_ - nlim_ < *(NACT)) i_ = (ACT)[q_ - nlim_];                     \
+            const int i = i_;                                                                   \
+            if (i >= 0 && (CNT)[i] <= (MAXN)) { __VA_ARGS__ }                                   \
+        } else {                                                                                \
+            const int no = *(OVF).count;                                                        \
+            for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < no; q += gridDim.x * blockDim.x) { \
+                const int i = (OVF).list[q];                                                    \
+                if (i >= (BASE) && i < (N)) { __VA_ARGS__ }                                     \
+            }                                                                                   \
+        }                                                                                       \
+    } while (0)
+
 // Persistent per-particle state of the FP32-mixed form.
 struct P32 {
     float4* hi;     // (hx, hy, hz, type word)
@@ -487,6 +509,7 @@ struct Fp32State {
     int *cell_of = nullptr, *rank = nullptr, *perm = nullptr, *tiles = nullptr, *err = nullptr;
     int *cells_d = nullptr, *cells_s = nullptr, *ncells = nullptr;  // non-empty cells (dynamic, static)
     int *ovf_list = nullptr, *novf = nullptr;  // particles whose neighbours exceed the list capacity
+    int *sact = nullptr, *nsact = nullptr;     // static-block particles with a non-empty list
     unsigned* maxdisp = nullptr;               // squared displacement since the last list build
     bool built = false;
     double* stage = nullptr;       // f64 export staging (9 n)
