@@ -186,29 +186,34 @@ def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None):
     a re-read).  FP64 (cell traversal, no lists): rates read x (24) + m_V (8) + v_tmp (24) +
     density_tmp (8) + pressure (8) + mat_type (4) + f32 prefilter position (16) of every
     particle, and per flow particle its CSPM matrix (72 when corrected) plus the writes of
-    d_density (8) and d_vel (24).  FP32-mixed:
-      rates:  hi + lo + (v_tmp, p / rho^2) of every particle (48); per flow particle
-              density_tmp (4) + list count (4) + CSPM matrix (36 when corrected) + writes
-              d_density (4) and d_vel (16); plus the real particles' list entries;
-      corr:   hi + lo + count of every particle (36) + writes CSPM_f (4) and CSPM_L (36 when
-              corrected); plus every list entry;
-      boundary: per dummy hi + lo + velocity (48) + count (4) + writes (v_tmp, p) (16),
-              (p, rho) (8), density_tmp (4), pressure (4); per flow particle m_V + v_tmp +
-              (p, rho) (4 + 16 + 8); plus the dummies' list entries.
+    d_density (8) and d_vel (24).  FP32-mixed (n_vis = flow particles + dummies with a
+    non-empty list, the particles the list kernels visit; WCSPH scenes have no other real
+    particles):
+      rates:  lo (position offset, m_V) + (v_tmp, p / rho^2) of every visited particle (32);
+              per flow particle its hi (16), density_tmp (4), list count (4), CSPM matrix
+              (24, six planes, when corrected) and the writes of d_density (4) and d_vel
+              (16); plus the flow particles' list entries;
+      corr:   hi + lo + count of every visited particle (36), the listed dummies' index (4),
+              writes CSPM_f (4) and CSPM_L (24 when corrected); plus every list entry;
+      boundary: per listed dummy its index (4), hi + lo + velocity (48), count (4),
+              CSPM_f (4) and the writes (v_tmp, p / rho^2) (16), (p, rho) (8),
+              density_tmp (4), pressure (4); per flow particle lo + v_tmp + (p, rho)
+              (16 + 16 + 8); plus the dummies' list entries.
     """
-    n_dummy = n_total - n_flow
     if precision == "fp64":
         if kernel != "rates":
             return None
         return n_total * 92 + n_flow * (4 + (72 if corr else 0) + 32)
     lists = lists or {"entries_real": 0, "entries_dummy": 0}
     er, ed = lists["entries_real"], lists["entries_dummy"]
+    na = lists.get("listed_dummies", n_total - n_flow)
+    n_vis = n_flow + na
     if kernel == "rates":
-        return n_total * 48 + n_flow * (4 + 4 + (36 if corr else 0) + 20) + 4 * er
+        return n_vis * 32 + n_flow * (16 + 4 + 4 + (24 if corr else 0) + 20) + 4 * er
     if kernel == "kernel_corr":
-        return n_total * (36 + 4 + (36 if corr else 0)) + 4 * (er + ed)
+        return n_vis * (36 + 4 + (24 if corr else 0)) + na * 4 + 4 * (er + ed)
     if kernel == "boundary":
-        return n_dummy * (48 + 4 + 32) + n_flow * 28 + 4 * ed
+        return na * (4 + 48 + 4 + 4 + 32) + n_flow * 40 + 4 * ed
     return None
 
 

@@ -191,10 +191,12 @@ int tsg_reduce_diag(tsg_handle* h, double out[8], void* stream);
  * traverses cells and keeps no lists): out[0] list entries stored for real particles
  * (pairs within the support plus the skin), out[1] the same for dummy / repulsive
  * particles, out[2] particles whose neighbours exceeded the list capacity (served by
- * direct traversal), out[3] list builds since upload.
+ * direct traversal), out[3] list builds since upload, out[4] dummy / repulsive particles
+ * with a non-empty list (the ones the per-step kernel correction and boundary
+ * extrapolation visit; the others keep the values written at the list build).
  * No reference counterpart (the reference re-walks the cells in every loop); used for
  * byte accounting and to report the rebuild rate.  Synchronises. */
-int tsg_list_stats(tsg_handle* h, int64_t out[4], void* stream);
+int tsg_list_stats(tsg_handle* h, int64_t out[5], void* stream);
 
 /* Device error word accumulated since the last call (and cleared).  Synchronises. */
 int tsg_last_error(tsg_handle* h, void* stream);

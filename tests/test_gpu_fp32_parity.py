@@ -80,6 +80,10 @@ def test_neighbor_sets_match(oracle_lib, native, scene):
             assert abs(r - R) < 1e-6 * R, f"pair ({oid[oi]}, {idn}) at r={r} differs"
             mismatched += 1
     assert mismatched <= 4
+    # the dummies visited per step: every dummy with a flow neighbour within R is listed
+    gmt = sim.ps.field("mat_type").cpu().numpy()
+    listed = sim.ps.list_stats()["listed_dummies"]
+    assert np.count_nonzero((gmt < 0) & (gc > 0)) <= listed <= np.count_nonzero(gmt < 0)
 
 
 def test_kernel_corr_close(oracle_lib, native):

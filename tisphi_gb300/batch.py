@@ -124,7 +124,7 @@ class SceneBatch:
             raise nat.NativeError(rc, "device error word")
 
     def list_stats(self):
-        out = np.zeros(4, dtype=np.int64)
+        out = np.zeros(5, dtype=np.int64)
         nat.check(self._lib.tsg_list_stats(self._h, nat.as_ptr(out, ctypes.c_int64), _stream()), "list_stats")
         return {"entries_real": int(out[0]), "entries_dummy": int(out[1]), "overflowed": int(out[2]),
-                "builds": int(out[3])}
+                "builds": int(out[3]), "listed_dummies": int(out[4])}

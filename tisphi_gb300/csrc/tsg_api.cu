@@ -662,7 +662,7 @@ int tsg_reduce_diag(tsg_handle* h, double out[8], void* stream) {
     return check_cuda();
 }
 
-int tsg_list_stats(tsg_handle* h, int64_t out[4], void* stream) {
+int tsg_list_stats(tsg_handle* h, int64_t out[5], void* stream) {
     if (!h || !out || !h->uploaded) return TSG_E_STATE;
     if (!use_fp32(h)) return TSG_E_UNSUPPORTED;
     int rc = fp32_list_stats(*h->f32, out, S(stream));

@@ -365,9 +365,11 @@ __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const fl
     });
 }
 
+// Real particles all live in the dynamic block (the static block holds fixed boundary
+// particles only), so the dynamic block is covered.
 __global__ void k_init_tmp32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) return;
+    if (i >= k.nd) return;
     const int ti = tf_type(p.hi[i].w);
     if (ti > 0) {
         const float4 v = p.vel[i];
@@ -1743,19 +1745,22 @@ void fp32_sort(Fp32State& st, cudaStream_t s) {
     ++st.rebuilds;
 }
 
-int fp32_list_stats(Fp32State& st, int64_t* out4, cudaStream_t s) {
+int fp32_list_stats(Fp32State& st, int64_t* out5, cudaStream_t s) {
     if (!st.built) return TSG_E_STATE;
     fp32_flush_counters(st, s);
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(st.scratch);
     cudaMemsetAsync(acc, 0, 3 * sizeof(unsigned long long), s);
     TSG_LAUNCH(k_list_stats, nblk(st.k.n), TPB, s, st.k, st.T.cnt, acc);
     unsigned long long h[3] = {0, 0, 0};
+    int nact = 0;
     cudaMemcpyAsync(h, acc, sizeof h, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&nact, st.nsact, sizeof nact, cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
-    out4[0] = (int64_t)h[0];
-    out4[1] = (int64_t)h[1];
-    out4[2] = (int64_t)h[2];
-    out4[3] = st.rebuilds;
+    out5[0] = (int64_t)h[0];
+    out5[1] = (int64_t)h[1];
+    out5[2] = (int64_t)h[2];
+    out5[3] = st.rebuilds;
+    out5[4] = nact;
     return 0;
 }
 
@@ -1833,7 +1838,7 @@ void fp32_kernel_corr(Fp32State& st, cudaStream_t s) {
 
 void fp32_init_tmp(Fp32State& st, cudaStream_t s) {
     PhaseScope ph(s, PH_INIT);
-    TSG_LAUNCH(k_init_tmp32, nblk(st.k.n), TPB, s, st.k, st.P[st.cur], st.T);
+    TSG_LAUNCH(k_init_tmp32, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T);
 }
 
 // mu(I) / Drucker-Prager one_step (eng/solver_sph_muI.py:62-131, eng/solver_sph_dp.py:210-274).

@@ -33,7 +33,7 @@ void fp32_diag(Fp32State& st, double* scratch, double* host_out8, cudaStream_t s
 int* fp32_err_ptr(Fp32State& st);
 // out[0] / out[1] list entries stored for the dynamic / static block, out[2] overflowed
 // particles, out[3] list builds since creation.
-int fp32_list_stats(Fp32State& st, int64_t* out4, cudaStream_t s);
+int fp32_list_stats(Fp32State& st, int64_t* out5, cudaStream_t s);
 
 // Graph mode: nsteps full steps replayed from captured graphs (the re-sort runs inside the
 // graph when the device-side displacement check asks for it).  TSG_E_STATE while

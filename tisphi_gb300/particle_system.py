@@ -212,11 +212,12 @@ class ParticleSystem:
 
     def list_stats(self):
         """FP32-mixed neighbour-list occupancy: entries of real / dummy particles, overflowed
-        particles and list builds since upload (raises for the FP64 form, which keeps no lists)."""
-        out = np.zeros(4, dtype=np.int64)
+        particles, list builds since upload and dummies with a non-empty list (raises for the
+        FP64 form, which keeps no lists)."""
+        out = np.zeros(5, dtype=np.int64)
         nat.check(self._lib.tsg_list_stats(self._h, nat.as_ptr(out, ctypes.c_int64), _stream()), "list_stats")
         return {"entries_real": int(out[0]), "entries_dummy": int(out[1]), "overflowed": int(out[2]),
-                "builds": int(out[3])}
+                "builds": int(out[3]), "listed_dummies": int(out[4])}
 
     def check_errors(self):
         """Raise when the device error word has bits set (synchronises)."""
