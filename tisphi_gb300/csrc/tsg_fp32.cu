@@ -1077,12 +1077,13 @@ __global__ void k_export_int(K32 k, P32 p, int what, int* out) {
 // Write a field from planar f64 staging (tsg_write).
 // Import of one field from a row-major f64 buffer (component q of particle i at
 // in[i * comps + q]).
+// Row-major input (device memory, or page-locked host memory read over the host link).
 __global__ void k_import(K32 k, P32 p, int what, const double* in) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
+    const double* r = in + (size_t)(what <= 1 ? 3 : 1) * i;
     switch (what) {
     case 0: {
-        const double* r = in + 3 * (size_t)i;
         float4 h = p.hi[i], l = p.lo[i];
         double x[3] = {r[0] - k.vs[0], r[1] - k.vs[1], r[2] - k.vs[2]};
         l.x = (float)(x[0] - (double)h.x); l.y = (float)(x[1] - (double)h.y); l.z = (float)(x[2] - (double)h.z);
@@ -1091,15 +1092,14 @@ __global__ void k_import(K32 k, P32 p, int what, const double* in) {
     }
     case 1: {
         float4 v = p.vel[i];
-        const double* r = in + 3 * (size_t)i;
         const double a = r[0], b = r[1], c = r[2];
         v.x = (float)a; v.y = (float)b; v.z = (float)c;
         p.vel[i] = v;
         if (p.vlo) p.vlo[i] = make_float4((float)(a - v.x), (float)(b - v.y), (float)(c - v.z), 0.f);
         break;
     }
-    case 2: if (tf_type(p.hi[i].w) > 0) p.drho[i] = (float)(in[i] - (double)k.rho0); break;
-    case 3: p.vel[i].w = (float)in[i]; break;
+    case 2: if (tf_type(p.hi[i].w) > 0) p.drho[i] = (float)(r[0] - (double)k.rho0); break;
+    case 3: p.vel[i].w = (float)r[0]; break;
     default: break;
     }
 }
@@ -2372,6 +2372,19 @@ void fp32_diag(Fp32State& st, double* /*scratch*/, double* host_out8, cudaStream
 
 int* fp32_err_ptr(Fp32State& st) { return st.err; }
 
+// Device address of a host buffer the GPU can read and write in place (page-locked host
+// memory: under unified addressing every page-locked allocation is mapped), else null.
+// Field transfers through such a buffer convert on the fly in one kernel pass over the
+// host link, with no staging copy.
+static void* mapped_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int fp32_write(Fp32State& st, const char* name, const void* src, bool from_device, cudaStream_t s) {
     const std::string f(name);
     int what = -1, comps = 1;
@@ -2381,13 +2394,17 @@ int fp32_write(Fp32State& st, const char* name, const void* src, bool from_devic
     else if (f == "pressure") what = 3;
     else return TSG_E_NAME;
     const size_t n = st.n;
-    double* buf = st.stage;
-    cudaMemcpyAsync(buf, src, sizeof(double) * comps * n, from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
-    TSG_LAUNCH(k_import, nblk(n), TPB, s, st.k, st.P[st.cur], what, buf);
+    const double* in = from_device ? nullptr : static_cast<const double*>(mapped_host(src));
+    if (!in) {
+        cudaMemcpyAsync(st.stage, src, sizeof(double) * comps * n,
+                        from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
+        in = st.stage;
+    }
+    TSG_LAUNCH(k_import, nblk(n), TPB, s, st.k, st.P[st.cur], what, in);
     if (what == 0) st.lists_valid = false;
-    // boundary particles without flow neighbours: their extrapolated state follows the
+    // boundary particles without flow neighbours: their extrapolated state follows an
     // imported velocity / pressure at once (it is otherwise written at list builds only)
-    if (st.built) static_active(st, s);
+    if (st.built && (what == 1 || what == 3)) static_active(st, s);
     return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
 }
 
@@ -2395,10 +2412,14 @@ int fp32_read(Fp32State& st, const char* name, void* dst, int mode, cudaStream_t
     const size_t n = st.n;
     const cudaMemcpyKind kind = mode == 1 ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     const int what = fp32_float_field(st, name);
-    if (what >= 0) {  // float fields: export straight into row-major staging, one copy
+    if (what >= 0) {  // float fields: export row-major into the destination or staging + one copy
         const int comps = fp32_field_comps(what);
-        TSG_LAUNCH(k_export, nblk(n), TPB, s, st.k, st.P[st.cur], st.T, what, st.stage, (size_t)1, (size_t)comps);
-        cudaMemcpyAsync(dst, st.stage, sizeof(double) * n * comps, kind, s);
+        // (host destinations go through staging and a copy: stores to host memory from the
+        // SMs run no faster than the copy engine over the host link)
+        double* out = mode == 1 ? static_cast<double*>(dst) : nullptr;
+        TSG_LAUNCH(k_export, nblk(n), TPB, s, st.k, st.P[st.cur], st.T, what, out ? out : st.stage, (size_t)1,
+                   (size_t)comps);
+        if (!out) cudaMemcpyAsync(dst, st.stage, sizeof(double) * n * comps, kind, s);
     } else {
         tsg_view v;
         int rc = fp32_field(st, name, &v, s);
