@@ -348,12 +348,14 @@ __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const fl
         const bool want_L = k.corr == 1 && flow_i;
         CSum s;
         float L[6] = {0, 0, 0, 0, 0, 0};
-        for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, flow_i,
-                          [&](int j, const float* d, float r2, int sidx, int tj, float mVj) {
+        const int ci = type_class(ti);
+        for_nbrs_g<DIM, FB, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, flow_i,
+                                  [](int) { return NoPayload{}; },
+                                  [&](int, const float* d, float r2, int sidx, int cj, float mVj, NoPayload) {
             const WG wg = w_pair<true, true, KT>(k, r2);
-            if (is_flow(tj)) s.add(mVj * wg.w);
-            if ((sidx & 7) == 7) s.flush();
-            if (want_L && tj == ti) {
+            if (code_flow(cj)) s.add(mVj * wg.w);
+            if (sidx % kFlushEvery == kFlushEvery - 1) s.flush();
+            if (want_L && cj == ci) {
                 const float gf = wg.g * mVj;
                 for (int a = 0; a < DIM; ++a)
                     for (int b = a; b < DIM; ++b) L[sym_idx(a, b)] += (-d[a]) * (gf * d[b]);
@@ -434,7 +436,7 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
                 bv[1].add(mw * vt.y);
                 if (DIM == 3) bv[2].add(mw * vt.z);
                 bp.add(mw * (pr.x + pr.y * k.g[1] * d[1]));
-                if ((sidx & 7) == 7) { bv[0].flush(); bv[1].flush(); bv[2].flush(); bp.flush(); }
+                if (sidx % kFlushEvery == kFlushEvery - 1) { bv[0].flush(); bv[1].flush(); bv[2].flush(); bp.flush(); }
             });
             (void)hi_i; (void)lo_i;
             const float f = t.cf[i];
@@ -471,9 +473,9 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         // viscosity factor for fluid and for boundary neighbours; -rho0 p_i / rho_i^2
         const float vf_f = visc_fac, vf_b = visc_fac * visc_b;
         const float pi_n = -k.rho0 * vti.w;
-        for_nbrs_g<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
-                            [&](int j) { return __ldg(t.vt + j); },
-                            [&](int, const float* d, float r2, int sidx, int tj, float mVj, const float4& vtj) {
+        for_nbrs_g<DIM, FB, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
+                                  [&](int j) { return __ldg(t.vt + j); },
+                                  [&](int, const float* d, float r2, int sidx, int cj, float mVj, const float4& vtj) {
             const WG wg = w_pair<false, true, KT>(k, r2);
             const float r = wg.r;
             const float mg = mVj * wg.g;   // m_Vj G, grad W = G d
@@ -491,10 +493,10 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
             // viscosity (fluid or boundary neighbours) and pressure, on the uncorrected gradient.
             // WCSPH scenes hold fluid, dummy, repulsive and rigid particles only (soil is rejected
             // at upload), so every non-fluid neighbour takes the boundary form
-            const float cv = (tj == MAT_FLUID ? vf_f : vf_b) * __fdividef(fminf(vdx, 0.f), r2 + k.eps_h2);
+            const float cv = (cj == kCodeFluid ? vf_f : vf_b) * __fdividef(fminf(vdx, 0.f), r2 + k.eps_h2);
             float sc = mg * (cv + fmaf(-k.rho0, vtj.w, pi_n));
             float rs = 0.f;
-            if (rep_on && tj == MAT_REP) {  // repulsive force (eng/solver_sph_base.py:675-689)
+            if (rep_on && cj == kCodeRep) {  // repulsive force (eng/solver_sph_base.py:675-689)
                 const float chi = (r > 0.f && r < k.diam) ? 1.f - r / k.diam : 0.f;
                 const float gm = r / k.h075;
                 float f = 0.f;
@@ -507,7 +509,7 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
             dv[0].add(sc * d[0]);
             dv[1].add(sc * d[1]);
             if (DIM == 3) dv[2].add(sc * d[2]);
-            if ((sidx & 7) == 7) { dd.flush(); dv[0].flush(); dv[1].flush(); dv[2].flush(); }
+            if (sidx % kFlushEvery == kFlushEvery - 1) { dd.flush(); dv[0].flush(); dv[1].flush(); dv[2].flush(); }
         });
         t.dd[i] = dd.get() * rti;
         t.dv[i] = make_float4(dv[0].get() + k.g[0], dv[1].get() + k.g[1],
@@ -545,7 +547,7 @@ __global__ void k_mui_stress32(K32 k, P32 p, T32 t, const float4* __restrict__ P
             float kc[3];
             grad_c<DIM, CORR>(L, w_grad(k, fast_sqrt(r2)), d, kc);
             vgrad_add<DIM>(mVj, vti, vli, t.vt[j], t.vtlo[j], kc, vg, dd);
-            if ((sidx & 7) == 7) dd.flush();
+            if (sidx % kFlushEvery == kFlushEvery - 1) dd.flush();
         });
         const size_t n = k.n;
         t.dd[i] = dd.get() * (k.rho0 + t.drt[i]);
@@ -589,7 +591,7 @@ __global__ void k_bdy_soil32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
                 bs[2] += mw * (t.sigt[2 * n + j] + (DIM == 3 ? rtj * k.g[2] * d[2] : 0.f));
                 bs[3] += mw * t.sigt[3 * n + j];
                 if (DIM == 3) { bs[4] += mw * t.sigt[4 * n + j]; bs[5] += mw * t.sigt[5 * n + j]; }
-                if ((sidx & 7) == 7) { bv[0].flush(); bv[1].flush(); bv[2].flush(); b1.flush(); b2.flush(); }
+                if (sidx % kFlushEvery == kFlushEvery - 1) { bv[0].flush(); bv[1].flush(); bv[2].flush(); b1.flush(); b2.flush(); }
             });
             const float f = t.cf[i];
             const float4 v = p.vel[i];
@@ -661,7 +663,7 @@ __global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
                 dv[1].add(rs * d[1]);
                 if (DIM == 3) dv[2].add(rs * d[2]);
             }
-            if ((sidx & 7) == 7) { dv[0].flush(); dv[1].flush(); dv[2].flush(); dd.flush(); }
+            if (sidx % kFlushEvery == kFlushEvery - 1) { dv[0].flush(); dv[1].flush(); dv[2].flush(); dd.flush(); }
         });
         const float damp = -k.damp_eps * sqrtf(k.damp_E / (rti * k.h2));
         t.dv[i] = make_float4(dv[0].get() + k.g[0] + damp * vti.x, dv[1].get() + k.g[1] + damp * vti.y,
@@ -928,7 +930,7 @@ __global__ void k_xsph32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, con
                 s[0].add(w * (vj.x - vi.x));
                 s[1].add(w * (vj.y - vi.y));
                 if (DIM == 3) s[2].add(w * (vj.z - vi.z));
-                if ((sidx & 7) == 7) { s[0].flush(); s[1].flush(); s[2].flush(); }
+                if (sidx % kFlushEvery == kFlushEvery - 1) { s[0].flush(); s[1].flush(); s[2].flush(); }
             });
             t.xs[i] = make_float4(s[0].get(), s[1].get(), DIM == 3 ? s[2].get() : 0.f, 0.f);
         }

@@ -44,17 +44,24 @@ constexpr int kMaxScenes = 4096;
 __device__ __forceinline__ bool is_flow(int t) { return t == MAT_FLUID || t == MAT_SOIL; }
 
 // Neighbour-list entries pack the neighbour index (bits 0-22, so this form holds at most
-// 2^23 particles), its material type (bits 23-25: type + 2 for repulsive, dummy, fluid and
-// soil, 7 for rigid) and the offset (hi_i - hi_j) / Q + 1 of the two particles' quantised
-// positions per axis (bits 26-27, 28-29, 30-31; Q is at least one cell of the list grid,
-// so two listed particles are never more than one quantum apart, and hi only changes when
-// the lists are rebuilt).  A traversal therefore reads the neighbour's lo record and
-// nothing of its hi record, and decodes the entry with shifts, masks and one float add per
-// axis.
+// 2^23 particles), its material code (bits 23-25) and the offset (hi_i - hi_j) / Q + 1 of
+// the two particles' quantised positions per axis (bits 26-27, 28-29, 30-31; Q is at least
+// one cell of the list grid, so two listed particles are never more than one quantum
+// apart, and hi only changes when the lists are rebuilt).  A traversal therefore reads the
+// neighbour's lo record and nothing of its hi record, and decodes the entry with shifts,
+// masks and one float add per axis.
+// Material codes: repulsive 0, dummy 1, rigid 2, fluid 4, soil 5 (bit 2 = flow particle),
+// so the hot kernels test a neighbour's kind on the code itself.
 constexpr int kEntryBits = 23;
 constexpr int kEntryMask = (1 << kEntryBits) - 1;
-__device__ __forceinline__ int type_class(int t) { return t == MAT_RIGID ? 7 : t + 2; }
-__device__ __forceinline__ int class_type(int c) { return c == 7 ? MAT_RIGID : c - 2; }
+constexpr int kCodeRep = 0, kCodeFluid = 4;
+__device__ __forceinline__ int type_class(int t) {
+    return t == MAT_FLUID ? 4 : t == MAT_SOIL ? 5 : t == MAT_DUMMY ? 1 : t == MAT_REP ? 0 : 2;
+}
+__device__ __forceinline__ int class_type(int c) {
+    return c == 4 ? MAT_FLUID : c == 5 ? MAT_SOIL : c == 1 ? MAT_DUMMY : c == 0 ? MAT_REP : MAT_RIGID;
+}
+__device__ __forceinline__ bool code_flow(int c) { return (c & 4) != 0; }
 __device__ __forceinline__ int make_entry(int j, int tj, int ox, int oy, int oz) {
     return (int)((unsigned)j | ((unsigned)type_class(tj) << kEntryBits) | ((unsigned)(ox + 1) << 26) |
                  ((unsigned)(oy + 1) << 28) | ((unsigned)(oz + 1) << 30));
@@ -71,6 +78,9 @@ __device__ __forceinline__ int entry_of(const K32& k, int j, const float4& hi_i,
 }
 __device__ __forceinline__ int entry_index(const K32&, int e) { return e & kEntryMask; }
 
+// Block-compensated accumulator: plain partial sums, Kahan-folded every flush (the list
+// kernels flush after every kFlushEvery-th slot).
+constexpr int kFlushEvery = 16;
 // Block-compensated accumulator: plain partial sums, Kahan-folded every flush.
 struct CSum {
     float s = 0.f, c = 0.f, p = 0.f;
@@ -238,13 +248,14 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
 }
 
 // Iterate i's neighbour list (FB = false) or traverse its stencil directly (FB = true: the
-// particle's list overflowed).  body(j, d, r2, slot, type_j, m_V_j, g_j) gets the exact f32
+// particle's list overflowed).  body(j, d, r2, slot, type_j, m_V_j, g_j) (with CODE: the
+// neighbour's material code in place of its type) gets the exact f32
 // displacement x_i - x_j of every neighbour within the support and g_j = gather(j), the
 // neighbour's payload, loaded together with its lo record (before the support test, so the
 // two gathers overlap; the list's skin pairs load it for nothing).  Two neighbours per trip;
 // the next trip's two list entries are loaded before this trip's gathers, so the entry
 // stream (from DRAM) overlaps the gathers and the maths.
-template <int DIM, bool FB, class G, class F>
+template <int DIM, bool FB, bool CODE = false, class G, class F>
 __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
                                            const float4* __restrict__ HI, const float4* __restrict__ LO,
                                            const float4* __restrict__ PF, const int* __restrict__ dstart,
@@ -262,7 +273,8 @@ __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __res
             d[2] = DIM == 3 ? entry_offset(e, 2) * k.Q + (lo_i.z - l.z) : 0.f;
             float r2 = d[0] * d[0] + d[1] * d[1];
             if (DIM == 3) r2 += d[2] * d[2];
-            if (r2 < k.R2) body(e & kEntryMask, d, r2, s, class_type((e >> kEntryBits) & 7), l.w, g);
+            const int c = (e >> kEntryBits) & 7;
+            if (r2 < k.R2) body(e & kEntryMask, d, r2, s, CODE ? c : class_type(c), l.w, g);
         };
         int s = 0;
         int e0 = 0, e1 = 0;
@@ -289,7 +301,8 @@ __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __res
     } else {
         int s = 0;
         enum_neighbors<DIM>(k, i, HI, LO, PF, dstart, sstart, flow_i, [&](int j, const float* d, float r2) {
-            body(j, d, r2, s++, tf_type(HI[j].w), LO[j].w, gather(j));
+            const int tj = tf_type(HI[j].w);
+            body(j, d, r2, s++, CODE ? type_class(tj) : tj, LO[j].w, gather(j));
         });
     }
 }
