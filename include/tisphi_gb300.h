@@ -205,7 +205,10 @@ int tsg_last_error(tsg_handle* h, void* stream);
  * (cell-sorted) particle order.  The caller buffer is row-major (n, k) f64 for float fields
  * and int32 for integer fields; host buffers should be pinned for the copies to overlap.
  * Replaces the reference's from_numpy / to_numpy transfers (eng/particle_system.py:289-314,
- * :413-456).  tsg_read's to_device: 0 host destination (synchronises the stream), 1 device
+ * :413-456).  tsg_write with a page-locked host source (FP32-mixed form): the conversion
+ * kernel reads it in place, in stream order, so the caller keeps it unchanged until the
+ * stream has passed the call (as for an asynchronous copy from pinned memory).
+ * tsg_read's to_device: 0 host destination (synchronises the stream), 1 device
  * destination, 2 host destination without synchronising (several reads can then share one
  * synchronisation; the caller synchronises the stream before touching dst). */
 int tsg_write(tsg_handle* h, const char* name, const void* src, int from_device, void* stream);
