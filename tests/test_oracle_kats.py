@@ -1,0 +1,232 @@
+"""Known-answer tests of the f64 oracle (CPU), for properties the reference's formulas
+must have whatever the implementation:
+
+1. kernel normalisation: on an unjittered lattice, for a fluid particle whose whole support
+   is fluid, the oracle's Shepard sum and CSPM matrix equal an independent numpy lattice sum
+   of the reference's kernel formulas, and those sums show the kernels normalised (sum of
+   m_V W over the support, the particle itself included, is 1; the first moment
+   sum m_V (x_j - x_i) (x) grad W_ij is the identity) for the Wendland C2 and the cubic
+   spline kernel in 2D and the cubic spline in 3D; the reference's 3D Wendland C2 constant
+   integrates to 8 (eng/solver_sph_base.py:299-358, :386-423);
+2. grad W is odd: at uniform density and pressure the momentum equation gives an interior
+   particle of a symmetric lattice no net force, and pair forces cancel, so a fluid blob
+   without walls and gravity keeps its total momentum (eng/solver_sph_wc.py:34-71, :108-126);
+3. Drucker-Prager return mapping: after every step the stress lies inside or on the yield
+   surface, f <= eps_f, and the return-mapping flag written before the adaptation
+   matches f (eng/solver_sph_dp.py:60-118, :276-296);
+4. the counting sort is stable: particles end in flattened-cell order, and within a cell in
+   their previous order (eng/particle_system.py:228-252);
+5. hydrostatics: a water column at rest in a tank settles to p = rho0 |g| depth (time mean
+   of the pressure over 1,000 leap-frog steps after 1,000 steps of settling, least-squares
+   slope within 10 %; the weakly compressible column still rings, c = 18.7 m/s).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import cfg_of, small_column
+from tisphi_gb300 import scenes
+
+
+def _kernel(dim, kernel, h, r):
+    """W(r) and dW/dr of the reference's kernels (eng/solver_sph_base.py:299-358), numpy."""
+    q = r / h
+    if kernel == 1:  # Wendland C2, k = 7 / (4 pi h^2) or 21 / (2 pi h^3)
+        k = 7.0 / (4.0 * math.pi * h * h) if dim == 2 else 21.0 / (2.0 * math.pi * h ** 3)
+        q1 = np.clip(1.0 - 0.5 * q, 0.0, None)
+        return k * q1 ** 4 * (1.0 + 2.0 * q), k * q1 ** 3 * (-5.0 * q) / h
+    sig = (15.0 / (7.0 * math.pi) if dim == 2 else 3.0 / (2.0 * math.pi)) / h ** dim  # cubic spline
+    w = np.where(q <= 1.0, 2.0 / 3.0 - q * q + 0.5 * q ** 3, np.clip(2.0 - q, 0.0, None) ** 3 / 6.0)
+    dw = np.where(q <= 1.0, -2.0 * q + 1.5 * q * q, -0.5 * np.clip(2.0 - q, 0.0, None) ** 2)
+    return sig * w, sig * dw / h
+
+
+def _lattice_moments(dim, kernel, dx, h, R):
+    """Lattice sums over a full support: sum m_V W (self included) and
+    sum m_V (x_j - x_i) (x) grad W_ij, computed independently of the oracle."""
+    m = int(math.ceil(R / dx))
+    ax = np.arange(-m, m + 1) * dx
+    pts = np.stack(np.meshgrid(*([ax] * dim), indexing="ij"), -1).reshape(-1, dim)
+    r = np.linalg.norm(pts, axis=1)
+    keep = (r < R) & (r > 0)
+    d = -pts[keep]                       # x_i - x_j with x_i at the origin
+    w, dw = _kernel(dim, kernel, h, r[keep])
+    mv = dx ** dim
+    w0, _ = _kernel(dim, kernel, h, np.zeros(1))
+    total = mv * (w.sum() + w0[0])
+    grad = (dw / r[keep])[:, None] * d   # grad_i W_ij
+    M = mv * np.einsum("na,nb->ab", -d, grad)
+    return total, M
+
+
+def _lattice_scene(dim, kernel, corr=1):
+    if dim == 2:
+        d = scenes.dambreak_2d(spacing=0.02, width=0.6, height=0.4, domain=(1.2, 0.8), jitter=0.0,
+                               kernel=kernel, corr=corr)
+    else:
+        d = scenes.dambreak_3d(spacing=0.02, domain=(0.6, 0.4, 0.3), size=(0.3, 0.24, 0.24), jitter_frac=0.0,
+                               corr=corr)
+        d["Configuration"]["kernel"] = kernel
+    return d
+
+
+def _interior_fluid(orc, full):
+    """Fluid particles whose neighbours are all fluid and whose support is complete: all
+    `full` lattice points strictly inside the support radius are neighbours (lattice points
+    at the radius itself, where both kernels vanish, fall on either side by rounding)."""
+    counts, lst = orc.neighbors()
+    mt = orc.get("mat_type")
+    x = orc.get("x")
+    R = orc.scene.geom.support_radius
+    off = np.concatenate([[0], np.cumsum(counts)])
+    out = []
+    for i in np.nonzero(mt == 1)[0]:
+        nb = lst[off[i]:off[i + 1]]
+        inside = np.linalg.norm(x[nb] - x[i], axis=1) < R * (1.0 - 1e-6)
+        if np.all(mt[nb] == 1) and np.count_nonzero(inside) == full:
+            out.append(i)
+    return np.array(out, dtype=np.int64)
+
+
+@pytest.mark.parametrize("dim,kernel", [(2, 1), (2, 0), (3, 1), (3, 0)])
+def test_kernel_normalisation_and_first_moment(oracle_lib, dim, kernel):
+    cfg = cfg_of(_lattice_scene(dim, kernel))
+    orc = oracle_lib.OracleSim(cfg)
+    orc.sort()
+    orc.call(oracle_lib.ORC_KERNEL_CORR)
+    inner = _interior_fluid(orc, 24 if dim == 2 else 92)
+    assert inner.size > 10
+    g = orc.scene.geom
+    total, M = _lattice_moments(dim, kernel, g.particle_diameter, g.smoothing_len, g.support_radius)
+    # the kernels are normalised (the lattice quadrature of a support of 3 spacings is good
+    # to 1 %) - except the reference's 3D Wendland C2, whose constant 21 / (2 pi h^3)
+    # integrates to 8 over its support (21 / (16 pi h^3) would give 1): reproduced as written
+    # (the CSPM correction divides it out of the corrected gradient, the pressure and
+    # viscosity forces take it as it is) - and the oracle's sums equal the lattice sums
+    norm = 8.0 if (dim, kernel) == (3, 1) else 1.0
+    assert abs(total / norm - 1.0) < 1e-2 and np.max(np.abs(M / norm - np.eye(dim))) < 2e-2
+    mv = orc.get("m_V")[inner]
+    w0 = _kernel(dim, kernel, g.smoothing_len, np.zeros(1))[0][0]
+    shepard = 1.0 / orc.get("CSPM_f")[inner] + mv * w0
+    assert np.max(np.abs(shepard - total)) < 1e-12, f"sum m_V W = {shepard.min()}..{shepard.max()} vs {total}"
+    L = orc.get("CSPM_L")[inner][:, :dim, :dim]
+    Linv = np.linalg.inv(M)
+    assert np.max(np.abs(L - Linv)) < 1e-10, f"CSPM_L off the lattice inverse by {np.max(np.abs(L - Linv))}"
+
+
+def test_uniform_state_gives_no_interior_force_and_keeps_momentum(oracle_lib):
+    d = scenes.dambreak_2d(spacing=0.02, width=0.4, height=0.4, domain=(1.2, 1.2), jitter=0.0)
+    d["Configuration"]["gravitation"] = [0.0, 0.0, 0.0]
+    d["Configuration"]["boundary"] = 0            # no wall particles, no collision handling
+    d["Blocks"][0]["translation"] = [0.4, 0.4, 0.0]  # clear of the domain walls
+    cfg = cfg_of(d)
+    from tisphi_gb300.scene import build_scene
+    s = build_scene(cfg)
+    rho = 1.01 * 1000.0                            # uniform, above rho0: uniform pressure > 0
+    s.density[:] = rho
+    s.m_V[:] = s.mass / rho
+    rng = np.random.default_rng(3)
+    s.v[:, :2] = rng.normal(scale=0.1, size=(s.n, 2))
+    orc = oracle_lib.OracleSim(cfg, scene=s)
+    orc.sort()
+    orc.call(oracle_lib.ORC_KERNEL_CORR)
+    orc.call(oracle_lib.ORC_INIT_TMP)
+    orc.call(oracle_lib.ORC_ONE_STEP)
+    m = orc.get("mass")
+    dv = orc.get("d_vel")
+    assert np.all(orc.get("pressure") > 0)
+    p_tot = (m[:, None] * dv).sum(axis=0)
+    scale = np.abs(m[:, None] * dv).sum(axis=0).max()
+    assert np.max(np.abs(p_tot)) < 1e-12 * scale, f"momentum change {p_tot} of {scale}"
+    # the same state at rest: pressure alone, and an interior particle of the lattice feels
+    # no net force (grad W odd), while the free surface does
+    s2 = build_scene(cfg)
+    s2.density[:] = rho
+    s2.m_V[:] = s2.mass / rho
+    orc2 = oracle_lib.OracleSim(cfg, scene=s2)
+    orc2.sort()
+    orc2.call(oracle_lib.ORC_KERNEL_CORR)
+    orc2.call(oracle_lib.ORC_INIT_TMP)
+    orc2.call(oracle_lib.ORC_ONE_STEP)
+    inner = _interior_fluid(orc2, 24)
+    assert inner.size > 10
+    dv2 = orc2.get("d_vel")
+    surface = np.abs(dv2).max()
+    assert surface > 0 and np.max(np.abs(dv2[inner])) < 1e-9 * surface, \
+        f"interior force {np.max(np.abs(dv2[inner]))} against {surface} at the surface"
+
+
+def test_dp_stress_inside_yield_surface_after_each_step(oracle_lib):
+    d = small_column(3, integration=2)
+    cfg = cfg_of(d)
+    orc = oracle_lib.OracleSim(cfg)
+    mat = d["Materials"][0]
+    tf = math.tan(mat["friction"] / 180.0 * math.pi)
+    den = math.sqrt(9.0 + 12.0 * tf * tf)
+    alpha, k_c = tf / den, 3.0 * mat["cohesion"] / den
+    eps_f = 1e-4
+    seen = set()
+    for _ in range(15):
+        orc.step(1)
+        soil = orc.get("mat_type") == 2
+        st = orc.get("stress")[soil]
+        I1 = np.trace(st, axis1=1, axis2=2)
+        s = st - I1[:, None, None] / 3.0 * np.eye(3)
+        sJ2 = np.sqrt(0.5 * np.einsum("nij,nij->n", s, s))
+        f = sJ2 + alpha * I1 - k_c
+        scale = np.abs(st).max()
+        assert f.max() <= eps_f + 1e-12 * scale, f"f up to {f.max()}"
+        flag = orc.get("flag_retmap")[soil]
+        seen.update(np.unique(flag).astype(int).tolist())
+        # elastic before the adaptation stays untouched: f < -eps_f after it as well
+        assert np.all(f[flag == 0] < -eps_f)
+        # adapted particles (flags 2, 3) sit on the yield surface
+        adapted = (flag == 2) | (flag == 3)
+        if adapted.any():
+            assert np.max(np.abs(f[adapted])) < 1e-9 * scale
+    assert 0 in seen
+
+
+def test_counting_sort_is_stable(oracle_lib):
+    d = scenes.dambreak_2d(spacing=0.02, width=0.6, height=0.4, domain=(1.2, 0.8))
+    cfg = cfg_of(d)
+    orc = oracle_lib.OracleSim(cfg)
+    ids_before = orc.get("id0").astype(np.int64)
+    orc.sort()
+    g = orc.scene.geom
+    x = orc.get("x")
+    ids = orc.get("id0").astype(np.int64)
+    idx = np.floor((x - np.asarray(g.vdomain_start)) / g.grid_size).astype(np.int64)  # truncation, x >= vstart
+    ny, nz = int(g.grid_num[1]), int(g.grid_num[2])
+    flat = idx[:, 0] * ny * nz + idx[:, 1] * nz + (idx[:, 2] if g.dim == 3 else 0)
+    assert np.all(np.diff(flat) >= 0)
+    # stable: within a cell, the order before the sort (here id0 order)
+    rank_before = np.empty_like(ids_before)
+    rank_before[ids_before] = np.arange(ids_before.size)
+    same = np.diff(flat) == 0
+    assert np.all(np.diff(rank_before[ids])[same] > 0)
+    ends = orc.grid()
+    counts = np.bincount(flat, minlength=g.grid_num_total)
+    assert np.array_equal(np.cumsum(counts)[: g.grid_num_total], ends[: g.grid_num_total])
+
+
+def test_hydrostatic_column(oracle_lib):
+    d = scenes.dambreak_2d(spacing=0.01, width=0.2, height=0.1, domain=(0.2, 0.2), jitter=0.0)
+    orc = oracle_lib.OracleSim(cfg_of(d))
+    orc.step(1000)
+    n = orc.n
+    acc = np.zeros(n)
+    for _ in range(20):
+        orc.step(50)
+        ids = orc.get("id0").astype(np.int64)
+        acc[ids] += orc.get("pressure")
+    p_mean = acc / 20
+    ids = orc.get("id0").astype(np.int64)
+    fluid = np.zeros(n, dtype=bool)
+    fluid[ids] = orc.get("mat_type") == 1
+    y = np.zeros(n)
+    y[ids] = orc.get("x")[:, 1]
+    depth = y[fluid].max() - y[fluid]
+    slope = np.polyfit(depth, p_mean[fluid], 1)[0]
+    assert abs(slope / (1000.0 * 9.81) - 1.0) < 0.1, f"dp/ddepth = {slope:.1f} Pa/m"
