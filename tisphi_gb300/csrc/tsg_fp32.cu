@@ -367,16 +367,25 @@ __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const fl
     });
 }
 
+__device__ __forceinline__ float tait(const K32& k, float drt, float B);
+__device__ __forceinline__ void eos_store(const K32& k, P32& p, T32& t, int i, float w, float drt, float4 v3);
+
 // Real particles all live in the dynamic block (the static block holds fixed boundary
-// particles only), so the dynamic block is covered.
+// particles only), so the dynamic block is covered.  EOS: also the fluid's Tait pressure
+// from the new density_tmp (the first phase of the WCSPH one_step, fused here by the step
+// sequence; the same arithmetic as k_pre32).
+template <bool EOS>
 __global__ void k_init_tmp32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const int ti = tf_type(p.hi[i].w);
+    const float w = p.hi[i].w;
+    const int ti = tf_type(w);
     if (ti > 0) {
         const float4 v = p.vel[i];
-        t.vt[i] = make_float4(v.x, v.y, v.z, t.vt[i].w);
-        t.drt[i] = p.drho[i];
+        const float drt = p.drho[i];
+        t.drt[i] = drt;
+        if (EOS && ti == MAT_FLUID) eos_store(k, p, t, i, w, drt, v);
+        else t.vt[i] = make_float4(v.x, v.y, v.z, t.vt[i].w);
     }
     if (ti == MAT_SOIL && t.sigt) {
         const size_t n = k.n;
@@ -401,17 +410,22 @@ __device__ __forceinline__ float tait(const K32& k, float drt, float B) {
     return fmaxf(B * r, 0.f);
 }
 
+// Fluid pressure from density_tmp (WCSPH loop 1, eng/solver_sph_wc.py:86-90): p, p / rho^2
+// and (p, rho_tmp); v3 gives the v_tmp components stored beside p / rho^2.
+__device__ __forceinline__ void eos_store(const K32& k, P32& p, T32& t, int i, float w, float drt, float4 v3) {
+    const float pr = tait(k, drt, k.scene_par ? k.scene_par[tf_scene(w)].x : k.B);
+    const float rt = k.rho0 + drt;
+    p.vel[i].w = pr;
+    t.vt[i] = make_float4(v3.x, v3.y, v3.z, pr / (rt * rt));
+    t.pr[i] = make_float2(pr, rt);
+}
+
 __global__ void k_pre32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
     const float w = p.hi[i].w;
     if (tf_type(w) != MAT_FLUID) return;
-    const float drt = t.drt[i];
-    const float pr = tait(k, drt, k.scene_par ? k.scene_par[tf_scene(w)].x : k.B);
-    const float rt = k.rho0 + drt;
-    p.vel[i].w = pr;
-    t.vt[i].w = pr / (rt * rt);
-    t.pr[i] = make_float2(pr, rt);
+    eos_store(k, p, t, i, w, t.drt[i], t.vt[i]);
 }
 
 // Boundary extrapolation for dummy / repulsive / rigid particles in [base, base + count_n) (WC).
@@ -784,10 +798,12 @@ __global__ void k_geostatic32(K32 k, P32 p, const double* ymax, double K0) {
 }
 
 // ---------------------------------------------------------------- integrators
+template <bool EOS>
 __global__ void k_advect_half32(K32 k, P32 p, T32 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
-    const int ti = tf_type(p.hi[i].w);
+    const float wi = p.hi[i].w;
+    const int ti = tf_type(wi);
     if (ti <= 0) return;
     if (ti == MAT_SOIL && k.solver == 3) {
         const size_t n = k.n;
@@ -807,7 +823,8 @@ __global__ void k_advect_half32(K32 k, P32 p, T32 t) {
     } else {
         vt.x += k.hdt * dv.x; vt.y += k.hdt * dv.y; vt.z += k.hdt * dv.z;
     }
-    t.vt[i] = vt;
+    if (EOS && ti == MAT_FLUID) eos_store(k, p, t, i, wi, drt, vt);  // the next one_step's first phase
+    else t.vt[i] = vt;
 }
 
 // ---- RK4 (eng/solver_sph_base.py:134-180): accumulate m * rates over the four one_steps;
@@ -1840,7 +1857,7 @@ void fp32_kernel_corr(Fp32State& st, cudaStream_t s) {
 
 void fp32_init_tmp(Fp32State& st, cudaStream_t s) {
     PhaseScope ph(s, PH_INIT);
-    TSG_LAUNCH(k_init_tmp32, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T);
+    TSG_LAUNCH(k_init_tmp32<false>, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T);
 }
 
 // mu(I) / Drucker-Prager one_step (eng/solver_sph_muI.py:62-131, eng/solver_sph_dp.py:210-274).
@@ -1884,7 +1901,9 @@ void soil_one_step(Fp32State& st, cudaStream_t s) {
     }
 }
 
-void fp32_one_step(Fp32State& st, cudaStream_t s) {
+// eos = false: the fluid pressures were computed by the kernel before (the step sequence
+// fuses them into init_real2tmp and the leap-frog half step).
+static void one_step(Fp32State& st, cudaStream_t s, bool eos) {
     const K32& k = st.k;
     P32& p = st.P[st.cur];
     if (k.solver != 1) {
@@ -1892,7 +1911,7 @@ void fp32_one_step(Fp32State& st, cudaStream_t s) {
         else soil_one_step<3>(st, s);
         return;
     }
-    {
+    if (eos) {
         PhaseScope ph(s, PH_PRE);
         TSG_LAUNCH(k_pre32, nblk(k.nd), TPB, s, k, p, st.T);
     }
@@ -1915,12 +1934,14 @@ void fp32_one_step(Fp32State& st, cudaStream_t s) {
     }
 }
 
+void fp32_one_step(Fp32State& st, cudaStream_t s) { one_step(st, s, true); }
+
 void fp32_advect(Fp32State& st, int which, cudaStream_t s) {
     const K32& k = st.k;
     P32& p = st.P[st.cur];
     switch (which) {
     case TSG_ADVECT_FULL: { PhaseScope ph(s, PH_INTEGRATE); TSG_LAUNCH(k_advect_full32, nblk(k.nd), TPB, s, k, p, st.T, st.err); break; }
-    case TSG_ADVECT_LF_HALF: { PhaseScope ph(s, PH_INTEGRATE); TSG_LAUNCH(k_advect_half32, nblk(k.nd), TPB, s, k, p, st.T); break; }
+    case TSG_ADVECT_LF_HALF: { PhaseScope ph(s, PH_INTEGRATE); TSG_LAUNCH(k_advect_half32<false>, nblk(k.nd), TPB, s, k, p, st.T); break; }
     case TSG_ADVECT_POS: {
         PhaseScope ph(s, PH_POS);
         if (k.xsph) {
@@ -1966,7 +1987,15 @@ void fp32_rk_update(Fp32State& st, int m, cudaStream_t s) {
 // collision mode, enforce_boundary (eng/solver_sph_base.py:41-61, :79-120).
 void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
     fp32_kernel_corr(st, s);
-    fp32_init_tmp(st, s);
+    // WCSPH with symplectic Euler or leap-frog: the fluid EOS (first phase of each one_step)
+    // runs inside init_real2tmp and the half step, which produce its input density_tmp
+    const bool fuse = st.k.solver == 1 && st.c.ti != 4;
+    if (fuse) {
+        PhaseScope ph(s, PH_INIT);
+        TSG_LAUNCH(k_init_tmp32<true>, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T);
+    } else {
+        fp32_init_tmp(st, s);
+    }
     if (st.c.ti == 4) {
         fp32_advect(st, TSG_RK_INIT, s);
         const int m[4] = {1, 2, 2, 1};
@@ -1977,10 +2006,15 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
         }
         fp32_advect(st, TSG_RK_FINAL, s);
     } else {
-        fp32_one_step(st, s);
+        one_step(st, s, !fuse);
         if (st.c.ti == 2) {
-            fp32_advect(st, TSG_ADVECT_LF_HALF, s);
-            fp32_one_step(st, s);
+            if (fuse) {
+                PhaseScope ph(s, PH_INTEGRATE);
+                TSG_LAUNCH(k_advect_half32<true>, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T);
+            } else {
+                fp32_advect(st, TSG_ADVECT_LF_HALF, s);
+            }
+            one_step(st, s, !fuse);
         }
         fp32_advect(st, TSG_ADVECT_FULL, s);
     }
