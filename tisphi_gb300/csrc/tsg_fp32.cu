@@ -954,6 +954,9 @@ __global__ void k_xsph32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, con
     });
 }
 
+// POST: also the WCSPH density clamp of advect_something (k_post_wc32, which touches density
+// and m_V only, so its order against the position update does not matter).
+template <bool POST>
 __global__ void k_advect_pos32(K32 k, P32 p, T32 t, int* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
@@ -974,6 +977,11 @@ __global__ void k_advect_pos32(K32 k, P32 p, T32 t, int* err) {
         l.x += k.dt * v.x;
         l.y += k.dt * v.y;
         l.z += k.dt * v.z;
+    }
+    if (POST && tf_type(w) == MAT_FLUID) {
+        const float dr = fmaxf(p.drho[i], 0.f);
+        p.drho[i] = dr;
+        l.w = p.mass[i] / (k.rho0 + dr);
     }
     p.lo[i] = l;
     if (!(isfinite(l.x) && isfinite(l.y) && isfinite(l.z))) atomicOr(err, TSG_ERR_NONFINITE);
@@ -1936,28 +1944,34 @@ static void one_step(Fp32State& st, cudaStream_t s, bool eos) {
 
 void fp32_one_step(Fp32State& st, cudaStream_t s) { one_step(st, s, true); }
 
+// advect_pos with XSPH (eng/solver_sph_base.py:224-238); post: with the WCSPH density clamp
+// of advect_something fused in (the step sequence).
+static void advect_pos(Fp32State& st, cudaStream_t s, bool post) {
+    const K32& k = st.k;
+    P32& p = st.P[st.cur];
+    PhaseScope ph(s, PH_POS);
+    if (k.xsph) {
+        const Ovf ovf{st.ovf_list, st.novf};
+        if (k.dim == 2) {
+            TSG_LAUNCH((k_xsph32<2, false>), nblk(k.nd, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+            TSG_LAUNCH((k_xsph32<2, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+        } else {
+            TSG_LAUNCH((k_xsph32<3, false>), nblk(k.nd, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+            TSG_LAUNCH((k_xsph32<3, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+        }
+    }
+    if (post) TSG_LAUNCH(k_advect_pos32<true>, nblk(k.nd), TPB, s, k, p, st.T, st.err);
+    else TSG_LAUNCH(k_advect_pos32<false>, nblk(k.nd), TPB, s, k, p, st.T, st.err);
+    if (k.disp2_limit <= 0.f) st.lists_valid = false;
+}
+
 void fp32_advect(Fp32State& st, int which, cudaStream_t s) {
     const K32& k = st.k;
     P32& p = st.P[st.cur];
     switch (which) {
     case TSG_ADVECT_FULL: { PhaseScope ph(s, PH_INTEGRATE); TSG_LAUNCH(k_advect_full32, nblk(k.nd), TPB, s, k, p, st.T, st.err); break; }
     case TSG_ADVECT_LF_HALF: { PhaseScope ph(s, PH_INTEGRATE); TSG_LAUNCH(k_advect_half32<false>, nblk(k.nd), TPB, s, k, p, st.T); break; }
-    case TSG_ADVECT_POS: {
-        PhaseScope ph(s, PH_POS);
-        if (k.xsph) {
-            const Ovf ovf{st.ovf_list, st.novf};
-            if (k.dim == 2) {
-                TSG_LAUNCH((k_xsph32<2, false>), nblk(k.nd, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-                TSG_LAUNCH((k_xsph32<2, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-            } else {
-                TSG_LAUNCH((k_xsph32<3, false>), nblk(k.nd, st.tpb), st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-                TSG_LAUNCH((k_xsph32<3, true>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
-            }
-        }
-        TSG_LAUNCH(k_advect_pos32, nblk(k.nd), TPB, s, k, p, st.T, st.err);
-        if (k.disp2_limit <= 0.f) st.lists_valid = false;
-        break;
-    }
+    case TSG_ADVECT_POS: advect_pos(st, s, false); break;
     case TSG_ADVECT_SOMETHING: {
         PhaseScope ph(s, PH_POST);
         if (k.solver == 1) TSG_LAUNCH(k_post_wc32, nblk(k.nd), TPB, s, k, p);
@@ -2018,8 +2032,12 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
         }
         fp32_advect(st, TSG_ADVECT_FULL, s);
     }
-    fp32_advect(st, TSG_ADVECT_POS, s);
-    fp32_advect(st, TSG_ADVECT_SOMETHING, s);
+    if (st.k.solver == 1) {
+        advect_pos(st, s, true);  // advect_something of WCSPH is the density clamp, fused
+    } else {
+        advect_pos(st, s, false);
+        fp32_advect(st, TSG_ADVECT_SOMETHING, s);
+    }
     if (collide) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
 }
 
