@@ -456,6 +456,11 @@ int tsg_step(tsg_handle* h, int nsteps, void* stream) {
         // FP32-mixed with a neighbour skin re-sorts only when its lists expire
         if (!use_fp32(h) || fp32_rebuild_due(*h->f32, S(stream)))
             if ((rc = tsg_sort(h, stream))) return rc;
+        if (use_fp32(h)) {  // the kernel sequence the captured graphs replay, launched eagerly
+            fp32_step_body(*h->f32, collide, S(stream));
+            if ((rc = check_cuda())) return rc;
+            continue;
+        }
         if ((rc = tsg_kernel_corr(h, stream))) return rc;
         if ((rc = tsg_init_tmp(h, stream))) return rc;
         if ((rc = tsg_substep(h, stream))) return rc;

@@ -931,6 +931,42 @@ __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
     if (!isfinite(dr)) atomicOr(err, TSG_ERR_NONFINITE);
 }
 
+// WCSPH without XSPH, symplectic Euler or leap-frog: advect_SE / advect_LF, advect_pos and
+// the density clamp of advect_something in one pass over each particle's own state, in
+// the order of the separate kernels (the same arithmetic).
+__global__ void k_advect_final_wc32(K32 k, P32 p, T32 t, int* err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd) return;
+    const int ti = tf_type(p.hi[i].w);
+    if (ti <= 0) return;
+    float dr = p.drho[i] + k.dt * t.dd[i];
+    const bool dr_ok = isfinite(dr);
+    const float4 dv = t.dv[i];
+    float4 v = p.vel[i];
+    float4 vs = v;  // velocity the positions move with (v + vlo)
+    if (p.vlo) {
+        float4 vl = p.vlo[i];
+        two_sum_add(v.x, vl.x, k.dt * dv.x);
+        two_sum_add(v.y, vl.y, k.dt * dv.y);
+        two_sum_add(v.z, vl.z, k.dt * dv.z);
+        p.vlo[i] = vl;
+        vs = make_float4(v.x + vl.x, v.y + vl.y, v.z + vl.z, 0.f);
+    } else {
+        v.x += k.dt * dv.x; v.y += k.dt * dv.y; v.z += k.dt * dv.z;
+        vs = v;
+    }
+    p.vel[i] = v;
+    float4 l = p.lo[i];
+    l.x += k.dt * vs.x;
+    l.y += k.dt * vs.y;
+    l.z += k.dt * vs.z;
+    if (ti == MAT_FLUID) dr = fmaxf(dr, 0.f);
+    p.drho[i] = dr;
+    l.w = p.mass[i] / (k.rho0 + dr);
+    p.lo[i] = l;
+    if (!dr_ok || !(isfinite(l.x) && isfinite(l.y) && isfinite(l.z))) atomicOr(err, TSG_ERR_NONFINITE);
+}
+
 template <int DIM, bool FB>
 __global__ void k_xsph32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                          const int* __restrict__ sstart, Ovf ovf) {
@@ -2030,6 +2066,13 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
             }
             one_step(st, s, !fuse);
         }
+        if (fuse && !st.k.xsph) {  // advect_SE / _LF, advect_pos and the WCSPH clamp at once
+            PhaseScope ph(s, PH_INTEGRATE);
+            TSG_LAUNCH(k_advect_final_wc32, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T, st.err);
+            if (st.k.disp2_limit <= 0.f) st.lists_valid = false;
+            if (collide) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
+            return;
+        }
         fp32_advect(st, TSG_ADVECT_FULL, s);
     }
     if (st.k.solver == 1) {
@@ -2040,6 +2083,8 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
     }
     if (collide) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
 }
+
+void fp32_step_body(Fp32State& st, bool collide, cudaStream_t s) { f32::step_body(st, s, collide); }
 
 namespace {
 

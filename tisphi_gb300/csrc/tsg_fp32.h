@@ -21,6 +21,9 @@ void fp32_destroy(Fp32State* st);
 void fp32_sort(Fp32State& st, cudaStream_t s);
 // True when the neighbour lists must be rebuilt before the next step (always without a skin).
 bool fp32_rebuild_due(Fp32State& st, cudaStream_t s);
+// One step of the FP32-mixed sequence the captured graphs replay (kernel correction through
+// advect_something), launched eagerly; the caller re-sorts first when lists expire.
+void fp32_step_body(Fp32State& st, bool collide, cudaStream_t s);
 void fp32_kernel_corr(Fp32State& st, cudaStream_t s);
 void fp32_init_tmp(Fp32State& st, cudaStream_t s);
 void fp32_one_step(Fp32State& st, cudaStream_t s);

@@ -411,13 +411,15 @@ struct T32 {
 // f32 rounding noise of stored velocities (~1e-6 1/s of spurious strain rate) would set the
 // stress direction and its sensitivity to cohesion; keeping v as an unevaluated sum
 // hi + lo (two f32) makes velocity differences exact to ~1e-14 relative.
+// (hi, lo) += a with an error-free two-sum.  The additions are explicit round-to-nearest
+// operations: a contracted a = x * y into fma(x, y, hi) would break the error term.
 __device__ __forceinline__ void two_sum_add(float& hi, float& lo, float a) {
-    const float s = hi + a;
-    const float bb = s - hi;
-    const float e = (hi - (s - bb)) + (a - bb);
-    const float l = lo + e;
-    hi = s + l;
-    lo = l - (hi - s);
+    const float s = __fadd_rn(hi, a);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(a, bb));
+    const float l = __fadd_rn(lo, e);
+    hi = __fadd_rn(s, l);
+    lo = __fsub_rn(l, __fsub_rn(hi, s));
 }
 // (vj - vi) of two compensated velocities, component-wise.
 __device__ __forceinline__ float dv_comp(float hj, float lj, float hi_, float li) { return (hj - hi_) + (lj - li); }
