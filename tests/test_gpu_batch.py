@@ -8,6 +8,10 @@
 * One batch scene against the f64 oracle with the same tolerances.
 * Graph replay against the eager step path (per-phase profiling forces eager steps):
   bit-identical, since both launch the same kernels in the same order.
+* The step sequence (fluid EOS inside init_real2tmp and the leap-frog half step; advect,
+  advect_pos and the density clamp in one pass) against the reference's stages called one
+  by one (sort, calc_kernel_corr, init_real2tmp, substep, advect_pos, advect_something),
+  lists rebuilt every step: bit-identical.
 * Threads per block changes no arithmetic: bit-identical.  Cells per CTA of the list
   build (and the per-particle builder) give the same neighbour sets; the entries of a list
   may be ordered differently, so steps agree within 1e-6 relative.
@@ -147,6 +151,23 @@ def test_graph_replay_equals_eager(native):
         cnt = (ctypes.c_int64 * 16)()
         lib.tsg_profile_read(ms, cnt, len(nat.PHASES))
         lib.tsg_profile(0)
+    for nm in ("x", "v", "density", "pressure", "id0"):
+        np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy(), err_msg=nm)
+
+
+@pytest.mark.parametrize("ti", [1, 2])
+def test_step_sequence_equals_stage_calls(native, ti):
+    d = small_dambreak_2d(integration=ti)
+    d["Configuration"]["neighbourSkin"] = 0.0
+    a, b = _single(d), _single(d)
+    a.solver.step(6)
+    for _ in range(6):
+        b.ps.initialize_particle_system()
+        b.solver.calc_kernel_corr()
+        b.solver.init_real2tmp()
+        b.solver.substep()
+        b.solver.advect_pos()
+        b.solver.advect_something()
     for nm in ("x", "v", "density", "pressure", "id0"):
         np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy(), err_msg=nm)
 

@@ -925,7 +925,7 @@ __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
         two_sum_add(v.z, vl.z, k.dt * dv.z);
         p.vlo[i] = vl;
     } else {
-        v.x += k.dt * dv.x; v.y += k.dt * dv.y; v.z += k.dt * dv.z;
+        v.x = __fmaf_rn(k.dt, dv.x, v.x); v.y = __fmaf_rn(k.dt, dv.y, v.y); v.z = __fmaf_rn(k.dt, dv.z, v.z);
     }
     p.vel[i] = v;
     if (!isfinite(dr)) atomicOr(err, TSG_ERR_NONFINITE);
@@ -933,7 +933,9 @@ __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
 
 // WCSPH without XSPH, symplectic Euler or leap-frog: advect_SE / advect_LF, advect_pos and
 // the density clamp of advect_something in one pass over each particle's own state, in
-// the order of the separate kernels (the same arithmetic).
+// the order of the separate kernels.  The velocity and position updates are explicit fused
+// multiply-adds here and there, so the compiler's contraction choices cannot make the two
+// paths round differently.
 __global__ void k_advect_final_wc32(K32 k, P32 p, T32 t, int* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.nd) return;
@@ -952,14 +954,14 @@ __global__ void k_advect_final_wc32(K32 k, P32 p, T32 t, int* err) {
         p.vlo[i] = vl;
         vs = make_float4(v.x + vl.x, v.y + vl.y, v.z + vl.z, 0.f);
     } else {
-        v.x += k.dt * dv.x; v.y += k.dt * dv.y; v.z += k.dt * dv.z;
+        v.x = __fmaf_rn(k.dt, dv.x, v.x); v.y = __fmaf_rn(k.dt, dv.y, v.y); v.z = __fmaf_rn(k.dt, dv.z, v.z);
         vs = v;
     }
     p.vel[i] = v;
     float4 l = p.lo[i];
-    l.x += k.dt * vs.x;
-    l.y += k.dt * vs.y;
-    l.z += k.dt * vs.z;
+    l.x = __fmaf_rn(k.dt, vs.x, l.x);
+    l.y = __fmaf_rn(k.dt, vs.y, l.y);
+    l.z = __fmaf_rn(k.dt, vs.z, l.z);
     if (ti == MAT_FLUID) dr = fmaxf(dr, 0.f);
     p.drho[i] = dr;
     l.w = p.mass[i] / (k.rho0 + dr);
@@ -1010,9 +1012,9 @@ __global__ void k_advect_pos32(K32 k, P32 p, T32 t, int* err) {
         l.y += k.dt * (v.y + 0.5f * s.y);
         l.z += k.dt * (v.z + 0.5f * s.z);
     } else {
-        l.x += k.dt * v.x;
-        l.y += k.dt * v.y;
-        l.z += k.dt * v.z;
+        l.x = __fmaf_rn(k.dt, v.x, l.x);
+        l.y = __fmaf_rn(k.dt, v.y, l.y);
+        l.z = __fmaf_rn(k.dt, v.z, l.z);
     }
     if (POST && tf_type(w) == MAT_FLUID) {
         const float dr = fmaxf(p.drho[i], 0.f);
