@@ -295,6 +295,12 @@ double tsg_batch_pitch(const tsg_handle* h);
  * construction; the differentiable rollout perturbs them. */
 int tsg_set_soil(tsg_handle* h, double friction, double cohesion);
 
+/* WCSPH fluid parameters of a created handle: Tait stiffness B (Pa) and kinematic
+ * viscosity, with the viscosity factor 2 (dim + 2) viscosity recomputed
+ * (eng/solver_sph_wc.py:12-28).  No reference counterpart (fixed at construction there);
+ * the differentiable WCSPH rollout perturbs them.  Not for batched ensembles. */
+int tsg_set_fluid(tsg_handle* h, double stiffness, double viscosity);
+
 /* Bitwise snapshots of the FP32-mixed particle state (every per-particle array that
  * carries from one step to the next, in the current particle order) into / from a device
  * buffer of tsg_snapshot_bytes(h) bytes.  After a load the next step re-sorts first, so
@@ -304,16 +310,18 @@ int64_t tsg_snapshot_bytes(tsg_handle* h);
 int tsg_snapshot_save(tsg_handle* h, void* dst, void* stream);
 int tsg_snapshot_load(tsg_handle* h, const void* src, void* stream);
 
-/* Hand-written adjoint of one FP32-mixed mu(I) step (2D, symplectic Euler, no kernel
- * correction, dummy boundary, no XSPH; no reference counterpart - the reference's Taichi
- * kernels are not differentiated).  Call with the state loaded from the snapshot taken
- * before the step: it repeats the step's forward, then reverses it.  The adjoint arrays
- * are device f64 arrays in particle-id (id0) order, row-major: adj_x, adj_v, adj_v_tmp
- * (n, 3), adj_density (n,).  On entry they hold the adjoint of the state after the step
- * (x, v, density of soil particles; v_tmp of dummy particles, which the next step reads),
- * on return the adjoint of the state before it.  adj_params (device, 2 doubles) accumulates
- * d/d mu and d/d cohesion (mu = tan(friction)).  TSG_E_CAPACITY if a neighbour list
- * overflowed. */
+/* Hand-written adjoint of one FP32-mixed WCSPH or mu(I) step (2D, symplectic Euler, no
+ * kernel correction, dummy boundary, no XSPH, not a batched ensemble; no reference
+ * counterpart - the reference's Taichi kernels are not differentiated).  Call with the
+ * state loaded from the snapshot taken before the step: it repeats the step's forward, then
+ * reverses it.  The adjoint arrays are device f64 arrays in particle-id (id0) order,
+ * row-major: adj_x, adj_v, adj_v_tmp (n, 3), adj_density (n,).  On entry they hold the
+ * adjoint of the state after the step (x, v, density of the fluid / soil particles; for
+ * mu(I) also v_tmp of the dummy particles, which the next step reads - WCSPH recomputes it
+ * and returns zeros there), on return the adjoint of the state before it.  adj_params
+ * (device, 2 doubles) accumulates, for WCSPH, d/d B (Tait stiffness) and d/d nu' (the
+ * viscosity factor 2 (dim + 2) viscosity); for mu(I), d/d mu and d/d cohesion
+ * (mu = tan(friction)).  TSG_E_CAPACITY if a neighbour list overflowed. */
 int tsg_adjoint_step(tsg_handle* h, double* adj_x, double* adj_v, double* adj_density, double* adj_v_tmp,
                      double* adj_params, void* stream);
 

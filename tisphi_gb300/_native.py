@@ -83,6 +83,7 @@ SYMBOLS = {
     "tsg_visual": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp,
                                   ctypes.c_void_p]),
     "tsg_set_soil": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]),
+    "tsg_set_fluid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]),
     "tsg_snapshot_bytes": (ctypes.c_int64, [ctypes.c_void_p]),
     "tsg_snapshot_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "tsg_snapshot_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),

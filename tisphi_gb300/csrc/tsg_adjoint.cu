@@ -442,9 +442,258 @@ __global__ void k_copy_start(int n, P32 p, const float4* __restrict__ vt, Start 
     S.hi[i] = p.hi[i];
     S.lo[i] = p.lo[i];
     S.vel[i] = p.vel[i];
-    S.vlo[i] = p.vlo[i];
+    S.vlo[i] = p.vlo ? p.vlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);  // WCSPH keeps no compensated velocity
     S.drho[i] = p.drho[i];
     S.vt[i] = vt[i];
+}
+
+// ================================================================ WCSPH
+// Adjoint of one FP32-mixed WCSPH step: 2D, symplectic Euler, no kernel-gradient
+// correction, dummy-particle boundary, no XSPH.  The step (eng/solver_sph_base.py:41-91,
+// :224-247, :386-398, :653-663; eng/solver_sph_wc.py:30-132) maps the fluid state (x, v, rho;
+// m_V = m / rho) to the next one through
+//   p_i   = max(B ((rho_i / rho0)^g - 1), 0),  P_i = p_i / rho_i^2                  (EOS)
+//   S_b   = sum_{fluid j} m_Vj W_bj,  cf_b = 1 / S_b                                (Shepard)
+//   U_b   = sum m_Vj v_j W_bj,  v~_b = 2 v_b - cf_b U_b
+//   Q_b   = sum m_Vj (p_j + rho_j g_y (y_b - y_j)) W_bj,  p_b = max(cf_b Q_b, 0),  P_b = p_b / rho0^2
+//   drho_i = rho_i sum_j m_Vj (v~_i - v~_j) . G_ij d_ij
+//   dv_i  = g + sum_j m_Vj [c_ij nu' min(u_ij . d_ij, 0) / (|d_ij|^2 + eps_h) - rho0 (P_i + P_j)] G_ij d_ij
+//           (u_ij = v~_i - v~_j, c_ij = 1 for fluid j and rho0 / rho_i for dummy j)
+//   rho'  = rho + dt drho,  v' = v + dt dv,  x' = x + dt v',  rho'' = max(rho', rho0)
+// The parameter adjoints are those of the Tait stiffness B and of nu' = 2 (d + 2) nu.
+// Kernel roles: WK0 end-of-step adjoint in and the update reversed; WK1 the pair terms of
+// continuity and momentum (both sides, gathered at each particle); WK2 the boundary
+// extrapolation reversed at each dummy; WK3 its terms gathered at each fluid particle; WK4
+// the EOS and m_V = m / rho reversed, adjoint out.
+
+__device__ __forceinline__ bool fluid(float w) { return tf_type(w) == MAT_FLUID; }
+
+// dp / d rho of the Tait EOS at density deviation drt (0 where the pressure is clamped).
+__device__ __forceinline__ float tait_drho(const K32& k, float drt, float p) {
+    if (!(p > 0.f)) return 0.f;
+    const float a = 1.f + drt / k.rho0;
+    float pw = 1.f;
+    if (k.exponent_is_int && k.gamma_i >= 1)
+        for (int q = 1; q < k.gamma_i; ++q) pw *= a;
+    else
+        pw = powf(a, k.gamma - 1.f);
+    return k.B * k.gamma * pw / k.rho0;
+}
+
+__global__ void k_wadj_init(K32 k, P32 p, T32 t, Start S, A32 A, const double* __restrict__ ax,
+                            const double* __restrict__ av, const double* __restrict__ ar) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    const int c = p.ids[i].x;
+    A.x[i] = A.v[i] = A.dv[i] = A.vn[i] = A.b1[i] = f2(0.f, 0.f);
+    A.r[i] = A.mv[i] = A.rt[i] = A.dr[i] = A.b2[i] = A.bs[i] = A.dds[i] = 0.f;
+    A.gp[i] = make_double2(0.0, 0.0);
+    if (!fluid(S.hi[i].w)) return;
+    const float2 xb = f2((float)ax[3 * (size_t)c], (float)ax[3 * (size_t)c + 1]);
+    const float2 vb = f2((float)av[3 * (size_t)c], (float)av[3 * (size_t)c + 1]);
+    const float drho1 = S.drho[i] + k.dt * t.dd[i];    // before the density clamp
+    const float rb1 = drho1 > 0.f ? (float)ar[c] : 0.f;
+    const float2 vt = f2(vb.x + k.dt * xb.x, vb.y + k.dt * xb.y);  // x' = x + dt v'
+    A.x[i] = xb;
+    A.v[i] = vt;                                       // v' = v + dt dv
+    A.dv[i] = f2(k.dt * vt.x, k.dt * vt.y);
+    A.r[i] = rb1;                                      // rho' = rho + dt drho
+    A.dr[i] = k.dt * rb1;
+}
+
+// One pair's forward terms seen from the centre i (fluid) with neighbour j:
+// d = x_i - x_j, u = v~_i - v~_j, s = m_Vj [c nu' min(u.d, 0) / (r^2 + eps_h) - rho0 (P_i + P_j)].
+struct WPair {
+    float dx, dy, r, G, Gp, ux, uy, w, Vn, V, dVdw, s;  // Vn = V / nu'
+};
+__device__ __forceinline__ bool wpair(const K32& k, const Start& S, const T32& t, int i, int j, float mvj,
+                                      float rho_i, WPair& P) {
+    Pair q;
+    if (!pair(k, S, i, j, q)) return false;
+    P.dx = q.dx; P.dy = q.dy; P.r = q.r; P.G = q.G; P.Gp = q.Gp;
+    const float4 vi = t.vt[i], vj = t.vt[j];
+    P.ux = vi.x - vj.x;
+    P.uy = vi.y - vj.y;
+    P.w = P.ux * P.dx + P.uy * P.dy;
+    const float cij = fluid(S.hi[j].w) ? 1.f : k.rho0 / rho_i;
+    const float den = 1.f / (q.r * q.r + k.eps_h2);
+    const float cw = P.w < 0.f ? cij * mvj * den : 0.f;
+    P.Vn = cw * P.w;                 // c m_Vj min(w, 0) / (r^2 + eps_h)
+    P.dVdw = k.visc_fac * cw;
+    P.V = k.visc_fac * P.Vn;
+    P.s = P.V - k.rho0 * mvj * (vi.w + vj.w);
+    return true;
+}
+
+__global__ void k_wadj_pairs(K32 k, P32 p, T32 t, Start S, A32 A) {
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kk >= k.n) return;
+    const bool kf = fluid(S.hi[kk].w);
+    const float mvk = S.lo[kk].w;
+    const float rho_k = k.rho0 + t.drt[kk];
+    float2 ax = f2(0.f, 0.f), av = f2(0.f, 0.f);
+    float ar = 0.f, amv = 0.f, aP = 0.f;
+    double gnu = 0.0;
+    const float2 ak = A.dv[kk];
+    const float ck = A.dr[kk];
+    for_list(k, t, kk, [&](int j) {
+        const bool jf = fluid(S.hi[j].w);
+        if (kf) {  // kk the centre i, j the neighbour
+            WPair P;
+            if (wpair(k, S, t, kk, j, S.lo[j].w, rho_k, P)) {
+                const float mvj = S.lo[j].w;
+                const float gx = P.G * P.dx, gy = P.G * P.dy;
+                // continuity: rho_i m_Vj u . g
+                const float cm = ck * rho_k * mvj;
+                av.x += cm * gx; av.y += cm * gy;
+                const float cr = P.Gp / P.r * (P.ux * P.dx + P.uy * P.dy);
+                ax.x += cm * (P.G * P.ux + cr * P.dx);
+                ax.y += cm * (P.G * P.uy + cr * P.dy);
+                ar += ck * mvj * (P.ux * gx + P.uy * gy);
+                // momentum: s (a . g)
+                const float sb = ak.x * gx + ak.y * gy;
+                const float ca = P.Gp / P.r * (ak.x * P.dx + ak.y * P.dy);
+                ax.x += P.s * (P.G * ak.x + ca * P.dx);
+                ax.y += P.s * (P.G * ak.y + ca * P.dy);
+                if (P.w < 0.f) {
+                    av.x += sb * P.dVdw * P.dx; av.y += sb * P.dVdw * P.dy;
+                    const float e2 = 2.f * P.V / (P.r * P.r + k.eps_h2);
+                    ax.x += sb * (P.dVdw * P.ux - e2 * P.dx);
+                    ax.y += sb * (P.dVdw * P.uy - e2 * P.dy);
+                    gnu += (double)sb * P.Vn;
+                    if (!jf) ar += -sb * P.V / rho_k;
+                }
+                aP += -sb * k.rho0 * mvj;
+            }
+        }
+        if (jf) {  // j the centre i, kk the neighbour
+            const float rho_j = k.rho0 + t.drt[j];
+            WPair P;
+            if (wpair(k, S, t, j, kk, mvk, rho_j, P)) {  // d = x_j - x_kk, u = v~_j - v~_kk
+                const float2 aj = A.dv[j];
+                const float cj = A.dr[j];
+                const float gx = P.G * P.dx, gy = P.G * P.dy;
+                const float cm = cj * rho_j * mvk;
+                av.x -= cm * gx; av.y -= cm * gy;
+                const float cr = P.Gp / P.r * (P.ux * P.dx + P.uy * P.dy);
+                ax.x -= cm * (P.G * P.ux + cr * P.dx);
+                ax.y -= cm * (P.G * P.uy + cr * P.dy);
+                if (kf) amv += cj * rho_j * (P.ux * gx + P.uy * gy);
+                const float sb = aj.x * gx + aj.y * gy;
+                const float ca = P.Gp / P.r * (aj.x * P.dx + aj.y * P.dy);
+                ax.x -= P.s * (P.G * aj.x + ca * P.dx);
+                ax.y -= P.s * (P.G * aj.y + ca * P.dy);
+                if (P.w < 0.f) {
+                    av.x -= sb * P.dVdw * P.dx; av.y -= sb * P.dVdw * P.dy;
+                    const float e2 = 2.f * P.V / (P.r * P.r + k.eps_h2);
+                    ax.x -= sb * (P.dVdw * P.ux - e2 * P.dx);
+                    ax.y -= sb * (P.dVdw * P.uy - e2 * P.dy);
+                    if (kf) amv += sb * P.V / mvk;
+                }
+                aP += -sb * k.rho0 * mvk;
+                if (kf) amv += -sb * k.rho0 * (t.vt[j].w + t.vt[kk].w);
+            }
+        }
+    });
+    A.x[kk] = f2(A.x[kk].x + ax.x, A.x[kk].y + ax.y);
+    A.v[kk] = f2(A.v[kk].x + av.x, A.v[kk].y + av.y);  // fluid: v; dummy: its v~
+    A.rt[kk] += aP;                                      // P = p / rho^2
+    if (kf) {
+        A.r[kk] += ar;
+        A.mv[kk] += amv;
+        A.gp[kk].y += gnu;
+    }
+}
+
+// Boundary extrapolation reversed at each dummy: coefficients of its sums.
+__global__ void k_wadj_bdy(K32 k, P32 p, T32 t, Start S, A32 A) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= k.n || tf_type(S.hi[b].w) > 0 || t.cnt[b] == 0) return;
+    float2 U = f2(0.f, 0.f);
+    float Q = 0.f, Sb = 0.f;
+    for_list(k, t, b, [&](int j) {
+        if (!fluid(S.hi[j].w)) return;
+        float d[3];
+        delta<2>(S.hi[b], S.lo[b], S.hi[j], S.lo[j], d);
+        const float r2 = d[0] * d[0] + d[1] * d[1];
+        if (!(r2 < k.R2)) return;
+        const float mw = S.lo[j].w * w_val(k, fast_sqrt(r2));
+        const float4 v = t.vt[j];
+        const float2 pr = t.pr[j];
+        U.x += mw * v.x; U.y += mw * v.y;
+        Q += mw * (pr.x + pr.y * k.g[1] * d[1]);
+        Sb += mw;
+    });
+    const float cf = t.cf[b];
+    const float2 avt = A.v[b];                          // adjoint of v~_b
+    const float pb = A.rt[b] / (k.rho0 * k.rho0);       // P_b = p_b / rho0^2
+    const bool open = cf * Q > 0.f;
+    float cfb = -(avt.x * U.x + avt.y * U.y);
+    if (open) cfb += pb * Q;
+    A.b1[b] = f2(-cf * avt.x, -cf * avt.y);            // adjoint of U_b
+    A.b2[b] = open ? pb * cf : 0.f;                     // adjoint of Q_b
+    A.bs[b] = Sb != 0.f ? -cfb * cf * cf : 0.f;         // adjoint of S_b
+}
+
+// The boundary sums' terms gathered at each fluid particle.
+__global__ void k_wadj_bdy_fluid(K32 k, P32 p, T32 t, Start S, A32 A) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k.n || !fluid(S.hi[j].w)) return;
+    const float mvj = S.lo[j].w;
+    const float4 v = t.vt[j];
+    const float2 pr = t.pr[j];
+    float2 ax = f2(0.f, 0.f), av = f2(0.f, 0.f);
+    float amv = 0.f, ap = 0.f, ar = 0.f;
+    for_list(k, t, j, [&](int b) {
+        if (tf_type(S.hi[b].w) > 0) return;
+        float d[3];
+        delta<2>(S.hi[b], S.lo[b], S.hi[j], S.lo[j], d);  // d = x_b - x_j
+        const float r2 = d[0] * d[0] + d[1] * d[1];
+        if (!(r2 < k.R2)) return;
+        const float r = fast_sqrt(r2);
+        const float W = w_val(k, r), G = w_grad(k, r);
+        const float2 B1 = A.b1[b];
+        const float B2 = A.b2[b], BS = A.bs[b];
+        const float qj = pr.x + pr.y * k.g[1] * d[1];
+        const float coef = (B1.x * v.x + B1.y * v.y) + B2 * qj + BS;
+        amv += coef * W;
+        av.x += B1.x * mvj * W; av.y += B1.y * mvj * W;
+        ap += B2 * mvj * W;
+        ar += B2 * mvj * k.g[1] * d[1] * W;
+        const float wb = mvj * coef;
+        ax.x += -wb * G * d[0];
+        ax.y += -wb * G * d[1] - B2 * mvj * pr.y * k.g[1] * W;
+    });
+    A.x[j] = f2(A.x[j].x + ax.x, A.x[j].y + ax.y);
+    A.v[j] = f2(A.v[j].x + av.x, A.v[j].y + av.y);
+    A.mv[j] += amv;
+    A.dds[j] += ap;  // adjoint of p_j (the dummies' pressure sums)
+    A.r[j] += ar;
+}
+
+// EOS and m_V = m / rho reversed; adjoint out in canonical order.
+__global__ void k_wadj_out(K32 k, P32 p, T32 t, Start S, A32 A, double* __restrict__ ax, double* __restrict__ av,
+                           double* __restrict__ ar, double* __restrict__ avt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    const size_t c = (size_t)p.ids[i].x;
+    avt[3 * c] = avt[3 * c + 1] = avt[3 * c + 2] = 0.0;
+    if (!fluid(S.hi[i].w)) {
+        ax[3 * c] = ax[3 * c + 1] = ax[3 * c + 2] = 0.0;
+        av[3 * c] = av[3 * c + 1] = av[3 * c + 2] = 0.0;
+        ar[c] = 0.0;
+        return;
+    }
+    const float drt = t.drt[i];
+    const float rho = k.rho0 + drt;
+    const float pi = t.pr[i].x;
+    const float pbar = A.dds[i] + A.rt[i] / (rho * rho);  // p enters the dummies' sums and P
+    float r = A.r[i] + pbar * tait_drho(k, drt, pi) - A.rt[i] * 2.f * pi / (rho * rho * rho);
+    r -= A.mv[i] * p.mass[i] / (rho * rho);
+    if (pi > 0.f) A.gp[i].x += (double)pbar * pi / k.B;  // p is proportional to B
+    ax[3 * c] = A.x[i].x; ax[3 * c + 1] = A.x[i].y; ax[3 * c + 2] = 0.0;
+    av[3 * c] = A.v[i].x; av[3 * c + 1] = A.v[i].y; av[3 * c + 2] = 0.0;
+    ar[c] = r;
 }
 
 template <class T>
@@ -494,7 +743,8 @@ void fp32_free_adjoint(Fp32State& st) {
 int fp32_adjoint_step(Fp32State& st, double* ax, double* av, double* ar, double* avt, double* pbar,
                       cudaStream_t s) {
     const K32& k = st.k;
-    if (k.solver != 2 || k.dim != 2 || st.c.ti != 1 || k.corr != 0 || k.boundary != 2 || k.xsph)
+    if ((k.solver != 1 && k.solver != 2) || k.dim != 2 || st.c.ti != 1 || k.corr != 0 || k.boundary != 2 ||
+        k.xsph || k.scene_par)
         return TSG_E_UNSUPPORTED;
     if (st.c.n_bdy > st.n - st.nd) return TSG_E_UNSUPPORTED;  // rigid particles
     AdjBuffers* B = adj_buffers(st);
@@ -513,6 +763,15 @@ int fp32_adjoint_step(Fp32State& st, double* ax, double* av, double* ar, double*
     TSG_LAUNCH(k_copy_start, nb, TPB, s, st.n, p, st.T.vt, B->S);
     f32::step_body(st, s, false);
     // reverse sweep
+    if (k.solver == 1) {
+        TSG_LAUNCH(k_wadj_init, nb, TPB, s, k, p, st.T, B->S, B->A, ax, av, ar);
+        TSG_LAUNCH(k_wadj_pairs, nb, TPB, s, k, p, st.T, B->S, B->A);
+        TSG_LAUNCH(k_wadj_bdy, nb, TPB, s, k, p, st.T, B->S, B->A);
+        TSG_LAUNCH(k_wadj_bdy_fluid, nb, TPB, s, k, p, st.T, B->S, B->A);
+        TSG_LAUNCH(k_wadj_out, nb, TPB, s, k, p, st.T, B->S, B->A, ax, av, ar, avt);
+        TSG_LAUNCH(k_adj_params, 1, 256, s, st.n, B->A.gp, pbar);
+        return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
+    }
     TSG_LAUNCH(k_adj_init, nb, TPB, s, k, p, st.T, B->S, B->A, ax, av, ar, avt);
     TSG_LAUNCH(k_adj_mom, nb, TPB, s, k, p, st.T, B->S, B->A);
     TSG_LAUNCH(k_adj_bdy, nb, TPB, s, k, p, st.T, B->S, B->A);

@@ -755,6 +755,18 @@ int tsg_set_soil(tsg_handle* h, double friction, double cohesion) {
     return 0;
 }
 
+int tsg_set_fluid(tsg_handle* h, double stiffness, double viscosity) {
+    if (!h) return TSG_E_ARG;
+    Consts& c = h->c;
+    if (c.solver != 1 || h->nscenes > 0) return TSG_E_UNSUPPORTED;
+    h->cfg.stiffness = stiffness;
+    h->cfg.viscosity = viscosity;
+    c.B = stiffness;
+    c.visc_fac = 2 * (c.dim + 2) * viscosity;
+    if (use_fp32(h)) fp32_set_fluid(*h->f32, c);
+    return 0;
+}
+
 int64_t tsg_snapshot_bytes(tsg_handle* h) {
     if (!h || !h->uploaded || !use_fp32(h)) return 0;
     return (int64_t)fp32_snapshot_bytes(*h->f32);

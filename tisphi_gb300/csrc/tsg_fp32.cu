@@ -2331,6 +2331,13 @@ void fp32_set_soil(Fp32State& st, const Consts& c) {
         if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
 }
 
+void fp32_set_fluid(Fp32State& st, const Consts& c) {
+    st.k.B = (float)c.B;
+    st.k.visc_fac = (float)c.visc_fac;
+    for (auto& g : st.graphs)  // the captured launches hold the constants by value
+        if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+}
+
 // Coordinate search over the launch parameters, each candidate timed from the same saved
 // state: threads per block of the neighbour kernels (full steps), cells per CTA of the
 // list build (re-sort + build), steps per graph launch (full steps).  The state is put

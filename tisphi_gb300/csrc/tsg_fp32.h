@@ -56,6 +56,7 @@ int fp32_snapshot_copy(Fp32State& st, void* buf, bool load, cudaStream_t s);
 // Replace the granular material constants (mu(I): tan(friction), cohesion; Drucker-Prager:
 // the yield-surface constants) of a created state; captured graphs are dropped.
 void fp32_set_soil(Fp32State& st, const Consts& c);
+void fp32_set_fluid(Fp32State& st, const Consts& c);
 // Adjoint of one mu(I) symplectic-Euler step from the loaded state (tsg_adjoint.cu).
 int fp32_adjoint_step(Fp32State& st, double* ax, double* av, double* ar, double* avt, double* pbar,
                       cudaStream_t s);
