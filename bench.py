@@ -453,6 +453,8 @@ def run_ours(args):
     }
     if "fp32_mixed" in forms and "fp64" in forms and "value" in forms["fp32_mixed"] and "value" in forms["fp64"]:
         line["speedup_fp32_mixed_vs_fp64"] = forms["fp32_mixed"]["value"] / forms["fp64"]["value"]
+    # the same rate counted over every particle of the step (fluid + dummies)
+    line["particle_updates_per_s_all_particles"] = h["n_total"] * ws / (h["ms_per_step"] * 1e-3)
     if rank == 0 and head == "fp32_mixed" and args.workload == "3d" and not args.no_full_run:
         line["forms"]["fp32_mixed"]["full_1000_step_run"] = full_run(cfg_dict)
     if rank == 0 and not args.no_errors and all("value" in forms.get(p, {}) for p in ("fp32_mixed", "fp64")):
