@@ -8,7 +8,7 @@
 // and runs each loop with OpenMP.  Every sum over neighbours is accumulated by one thread
 // in the reference's traversal order, so results do not depend on the thread count.
 //
-// Semantics fixed where the reference is racy or undefined (documented in the design doc):
+// Semantics fixed where the reference is racy or undefined:
 //  * counting sort is stable (the serial order of eng/particle_system.py:240-245);
 //  * a neighbour cell whose flattened index is outside [0, G) is skipped; a particle whose
 //    own flattened index is outside [0, G) is binned after every cell and flagged;
