@@ -1,8 +1,8 @@
 """ORACLE - test infrastructure only.
 
 ctypes front end of the f64 CPU oracle (sph_oracle.cpp).  Only tests/,
-``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this module, and only
-as the checker; the product package never does.
+``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this module, to check
+results or to time the CPU restatement; the product package never does.
 
 ``OracleSim(cfg)`` builds the initial particle arrays with the same host-side scene
 builder every implementation uses, derives the solver's constants the way the reference's

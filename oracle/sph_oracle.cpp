@@ -1,6 +1,6 @@
 // ORACLE - test infrastructure only.  Never linked into, loaded by or called from the
 // product path (tisphi_gb300/).  Only tests/, __graft_entry__.smoke() and bench.py's
-// CPU-baseline leg use it, as the checker.
+// CPU-baseline leg use it, to check results or to time the CPU restatement.
 //
 // f64 CPU restatement of the reference's per-substep SPH path (Rabmelon/tiSPHi, Taichi).
 // The reference keeps one array of structs (eng/particle_func.py:10-88) and runs every
