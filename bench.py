@@ -342,8 +342,8 @@ def error_report(cfg_dict, checkpoints=(1, 20)):
         torch.cuda.synchronize()
         rec = compare.field_errors(sims["fp32_mixed"].ps, sims["fp64"].ps)
         dr = {p: compare.drift(d0[p], s.ps.diagnostics()) for p, s in sims.items()}
-        rec["conservation"] = {p: {"mass_rel": v["mass_rel"], "energy_rel": v["energy_rel"],
-                                   "front": v["front"]} for p, v in dr.items()}
+        rec["conservation"] = {p: {"mass_rel": v["mass_rel"], "momentum_change": v["momentum"],
+                                   "energy_rel": v["energy_rel"], "front": v["front"]} for p, v in dr.items()}
         out[f"after_{n}_steps"] = rec
     del sims
     torch.cuda.synchronize()
@@ -623,6 +623,32 @@ def run_adjoint(args):
     print(json.dumps(line))
 
 
+def run_rollout(args):
+    """The 3D dambreak of the benchmark (block, domain, CSPM, leap-frog at dt 2e-5) at twice
+    the spacing (0.0108 m, one eighth of the particles) for 2,000 steps in both forms: the
+    FP32-mixed form's per-field error and conservation figures against the FP64 form after
+    1, 100 and 2,000 steps (mass, momentum and mechanical-energy change, dambreak front)."""
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    from tisphi_gb300 import build_native, scenes
+    build_native.build()
+    d = scenes.dambreak_3d(spacing=0.0108)
+    t0 = time.perf_counter()
+    rep = error_report(d, checkpoints=(1, 100, 2000))
+    wall = time.perf_counter() - t0
+    last = rep["after_2000_steps"]
+    c32, c64 = last["conservation"]["fp32_mixed"], last["conservation"]["fp64"]
+    line = {"metric": "FP32-mixed vs FP64 after 2,000 steps, 3D WCSPH dambreak at spacing 0.0108 m",
+            "value": last["density"]["rms_rel"], "unit": "RMS relative density error after 2,000 steps",
+            "higher_is_better": False,
+            "front_difference_m": abs(c32["front"] - c64["front"]),
+            "energy_change_rel": {"fp32_mixed": c32["energy_rel"], "fp64": c64["energy_rel"]},
+            "momentum_change": {"fp32_mixed": c32["momentum_change"], "fp64": c64["momentum_change"]},
+            "errors": rep, "wall_s": wall, "data": "synthetic"}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank, ws, dist = dist_init(args)
     if rank != 0:
@@ -672,7 +698,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["both", "fp32_mixed", "fp64"], default="both")
-    ap.add_argument("--workload", choices=["3d", "2d", "batch", "adjoint"], default="3d")
+    ap.add_argument("--workload", choices=["3d", "2d", "batch", "adjoint", "rollout"], default="3d")
     ap.add_argument("--adjoint-steps", type=int, default=2000, help="rollout length for --workload adjoint")
     ap.add_argument("--scenes", type=int, default=256, help="ensemble size for --workload batch")
     ap.add_argument("--spacing", type=float, default=0.0054)
@@ -691,6 +717,8 @@ def main():
         run_batch(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "rollout":
+        run_rollout(args)
     else:
         run_ours(args)
 
