@@ -289,8 +289,7 @@ def measure(args, cfg_dict, precision, rank, dist):
             for k in ins:
                 ps.write_field(k, host[k])
             solver.step()
-            for k in outs:
-                ps.read_field(k, host[k], non_blocking=True)
+            ps.read_fields(outs, [host[k] for k in outs], non_blocking=True)
             torch.cuda.synchronize()  # the step's results are on the host before the next step
         torch.cuda.synchronize()
         el = max_over_ranks(dist, time.perf_counter() - t0)

@@ -213,6 +213,10 @@ int tsg_last_error(tsg_handle* h, void* stream);
  * synchronisation; the caller synchronises the stream before touching dst). */
 int tsg_write(tsg_handle* h, const char* name, const void* src, int from_device, void* stream);
 int tsg_read(tsg_handle* h, const char* name, void* dst, int to_device, void* stream);
+/* tsg_read of several fields in one call (count <= 8): the FP32-mixed form converts them
+ * in one pass over the particle state before the copies. */
+int tsg_read_fields(tsg_handle* h, int count, const char* const* names, void* const* dsts, int to_device,
+                    void* stream);
 
 /* Number of kernel launches this library has issued since it was loaded (all handles).
  * No reference counterpart: instrumentation for launch accounting. */

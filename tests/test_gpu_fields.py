@@ -49,3 +49,22 @@ def test_write_read_round_trip(native, precision):
         x[:, 1] += 1e-3
         ps.write_field("x", x)
         np.testing.assert_array_equal(ps.read_field("x", np.empty_like(x)), x)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
+def test_read_fields_equals_read_field(native, precision):
+    from tisphi_gb300.simulation import Simulation
+    sim = Simulation(cfg_of(small_dambreak_2d()), precision=precision)
+    sim.solver.step(3)
+    ps = sim.ps
+    names = ["x", "v", "density", "pressure", "d_vel"]
+    one = {nm: ps.read_field(nm, np.empty(ps.field(nm).shape, dtype=np.float64)) for nm in names}
+    dsts = [torch.empty(ps.field(nm).shape, dtype=torch.float64).pin_memory() for nm in names]
+    ps.read_fields(names, dsts, non_blocking=True)
+    torch.cuda.synchronize()
+    for nm, d in zip(names, dsts):
+        np.testing.assert_array_equal(d.numpy(), one[nm], err_msg=nm)
+    dev = [torch.empty(ps.field(nm).shape, dtype=torch.float64, device="cuda") for nm in names]
+    ps.read_fields(names, dev)
+    for nm, d in zip(names, dev):
+        np.testing.assert_array_equal(d.cpu().numpy(), one[nm], err_msg=nm)

@@ -98,6 +98,8 @@ SYMBOLS = {
     "tsg_batch_pitch": (ctypes.c_double, [ctypes.c_void_p]),
     "tsg_write": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "tsg_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "tsg_read_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                       ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]),
     "tsg_launch_count": (ctypes.c_int64, []),
     "tsg_profile": (ctypes.c_int, [ctypes.c_int]),
     "tsg_profile_read": (ctypes.c_int, [_dp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),

@@ -560,6 +560,20 @@ int tsg_write(tsg_handle* h, const char* name, const void* src, int from_device,
     return check_cuda();
 }
 
+int tsg_read_fields(tsg_handle* h, int count, const char* const* names, void* const* dsts, int to_device,
+                    void* stream) {
+    if (!h || !names || !dsts || count <= 0 || !h->uploaded) return TSG_E_ARG;
+    if (to_device < 0 || to_device > 2) return TSG_E_ARG;
+    cudaStream_t s = S(stream);
+    if (use_fp32(h)) return fp32_read_set(*h->f32, count, names, dsts, to_device, s);
+    for (int q = 0; q < count; ++q) {
+        const int rc = tsg_read(h, names[q], dsts[q], to_device == 0 ? 2 : to_device, stream);
+        if (rc) return rc;
+    }
+    if (to_device == 0) cudaStreamSynchronize(s);
+    return check_cuda();
+}
+
 int tsg_read(tsg_handle* h, const char* name, void* dst, int to_device, void* stream) {
     if (!h || !name || !dst || !h->uploaded) return TSG_E_ARG;
     cudaStream_t s = S(stream);

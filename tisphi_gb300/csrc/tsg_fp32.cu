@@ -1071,11 +1071,9 @@ __global__ void k_enforce32(K32 k, P32 p) {
 // ---------------------------------------------------------------- export / diagnostics
 // Export of one field in f64: component q of particle i goes to out[q * sq + i * si]
 // (planar views: sq = n, si = 1; row-major host buffers: sq = 1, si = components).
-__global__ void k_export(K32 k, P32 p, T32 t, int what, double* out, size_t sq, size_t si) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) return;
+__device__ __forceinline__ void export_one(const K32& k, const P32& p, const T32& t, int what, int i, double* o,
+                                           size_t sq) {
     const size_t n = k.n;
-    double* o = out + (size_t)i * si;
     switch (what) {
     case 0: {  // x
         float4 h = p.hi[i], l = p.lo[i];
@@ -1122,6 +1120,26 @@ __global__ void k_export(K32 k, P32 p, T32 t, int what, double* out, size_t sq, 
     case 18: o[0] = t.deep[i]; break;
     default: break;
     }
+}
+
+__global__ void k_export(K32 k, P32 p, T32 t, int what, double* out, size_t sq, size_t si) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    export_one(k, p, t, what, i, out + (size_t)i * si, sq);
+}
+
+// Several float fields in one pass, field q row-major at out + off[q].
+struct ExportSet {
+    int count;
+    int what[8];
+    int comps[8];
+    size_t off[8];
+};
+__global__ void k_export_set(K32 k, P32 p, T32 t, ExportSet es, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    for (int q = 0; q < es.count; ++q)
+        export_one(k, p, t, es.what[q], i, out + es.off[q] + (size_t)i * es.comps[q], 1);
 }
 
 __global__ void k_export_int(K32 k, P32 p, int what, int* out) {
@@ -2513,6 +2531,36 @@ int fp32_write(Fp32State& st, const char* name, const void* src, bool from_devic
     // boundary particles without flow neighbours: their extrapolated state follows an
     // imported velocity / pressure at once (it is otherwise written at list builds only)
     if (st.built && (what == 1 || what == 3)) static_active(st, s);
+    return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
+}
+
+int fp32_read_set(Fp32State& st, int count, const char* const* names, void* const* dsts, int mode,
+                  cudaStream_t s) {
+    if (count <= 0 || count > 8) return TSG_E_ARG;
+    const size_t n = st.n;
+    ExportSet es{};
+    es.count = count;
+    size_t total = 0;
+    for (int q = 0; q < count; ++q) {
+        const int what = fp32_float_field(st, names[q]);
+        if (what < 0) return TSG_E_NAME;
+        es.what[q] = what;
+        es.comps[q] = fp32_field_comps(what);
+        es.off[q] = total;
+        total += (size_t)es.comps[q] * n;
+    }
+    if (total > 9 * n) {  // more than the staging holds: one field at a time
+        for (int q = 0; q < count; ++q) {
+            const int rc = fp32_read(st, names[q], dsts[q], mode == 0 ? 2 : mode, s);
+            if (rc) return rc;
+        }
+    } else {
+        const cudaMemcpyKind kind = mode == 1 ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        TSG_LAUNCH(k_export_set, nblk(n), TPB, s, st.k, st.P[st.cur], st.T, es, st.stage);
+        for (int q = 0; q < count; ++q)
+            cudaMemcpyAsync(dsts[q], st.stage + es.off[q], sizeof(double) * es.comps[q] * n, kind, s);
+    }
+    if (mode == 0) cudaStreamSynchronize(s);
     return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
 }
 

@@ -67,5 +67,7 @@ int fp32_write(Fp32State& st, const char* name, const void* src, bool from_devic
 // mode: 0 host destination (synchronises), 1 device destination, 2 host destination
 // without synchronising (the caller synchronises the stream before using dst).
 int fp32_read(Fp32State& st, const char* name, void* dst, int mode, cudaStream_t s);
+int fp32_read_set(Fp32State& st, int count, const char* const* names, void* const* dsts, int mode,
+                  cudaStream_t s);
 
 }  // namespace tsg

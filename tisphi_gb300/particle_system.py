@@ -155,6 +155,28 @@ class ParticleSystem:
         nat.check(self._lib.tsg_read(self._h, name.encode(), ctypes.c_void_p(ptr), mode, _stream()), f"read {name}")
         return dst
 
+    def read_fields(self, names, dsts, non_blocking=False):
+        """read_field for several fields in one call (the FP32-mixed form converts them in one
+        pass before the copies); the destinations are all host or all CUDA buffers."""
+        ptrs, devs = [], set()
+        for dst in dsts:
+            if isinstance(dst, torch.Tensor):
+                assert dst.is_contiguous()
+                ptrs.append(dst.data_ptr())
+                devs.add(int(dst.is_cuda))
+            else:
+                assert dst.flags.c_contiguous
+                ptrs.append(dst.ctypes.data)
+                devs.add(0)
+        if len(devs) != 1:
+            raise ValueError("read_fields: mixed host and device destinations")
+        dev = devs.pop()
+        mode = dev if dev or not non_blocking else 2
+        cnames = (ctypes.c_char_p * len(names))(*[nm.encode() for nm in names])
+        cptrs = (ctypes.c_void_p * len(ptrs))(*ptrs)
+        nat.check(self._lib.tsg_read_fields(self._h, len(names), cnames, cptrs, mode, _stream()), "read_fields")
+        return dsts
+
     @property
     def grid_particle_num(self):
         """Inclusive end offset of every cell after the last sort (host numpy, int32)."""
