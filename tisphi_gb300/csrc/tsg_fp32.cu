@@ -2,7 +2,7 @@
 //
 // Layout (unified particle index space, every array in the current sorted order):
 //   [0, nd)  dynamic block: real particles (fluid / soil / kinematic rigid), re-sorted by
-//            cell every step;
+//            cell whenever its neighbour lists expire;
 //   [nd, n)  static block: dummy and repulsive particles, which never move, sorted by cell
 //            once at upload.  Each block has its own cell table (exclusive starts, G + 2).
 // Positions are x - vdomain_start = hi + lo with hi an exact multiple of a power-of-two
@@ -12,15 +12,18 @@
 // Arithmetic is f32 except the cell index (f64, truncating cast as the reference,
 // eng/particle_system.py:216-218) and the FP64 conservation reductions.
 //
-// Neighbour lists: after the sort one kernel tests every candidate of the 3^dim stencil
-// (f32 prefilter on absolute positions, exact test on hi/lo inside a thin band) and writes
-// an ELL list per particle (slot-major, so a warp's reads coalesce).  Flow particles list
-// every neighbour; boundary and rigid particles list flow neighbours only (all their sums
-// run over flow particles).  Positions stay fixed until advect_pos, so the kernel
-// correction, both boundary passes and both rate passes of a leap-frog step reuse one list.
-// A particle whose count exceeds the capacity is handled by direct traversal.
+// Neighbour lists (Verlet lists of every pair within support + skin): after the sort one
+// kernel tests every candidate of the 3^dim stencil and writes an ELL list per particle
+// (slot-major, so a warp's reads coalesce) of 4-byte entries that carry the neighbour's
+// index, material code and quantised-position offset.  Flow particles list every
+// neighbour; boundary and rigid particles list flow neighbours only (all their sums run
+// over flow particles).  The lists are rebuilt (with the sort) once a particle has moved
+// 0.45 skin since the build; positions stay fixed until advect_pos, so every pass of a
+// step reuses one list.  A particle whose count exceeds the capacity is handled by direct
+// traversal.  Boundary particles with an empty list are written at the build and skipped
+// by the per-step kernels.
 //
-// Sums over neighbours are block-compensated: plain f32 sums over 8 neighbours, then a
+// Sums over neighbours are block-compensated: plain f32 sums over 16 neighbours, then a
 // Kahan update of the running total.
 //
 // Reference: eng/particle_system.py:228-269 (cell list), eng/solver_sph_base.py:41-238,
