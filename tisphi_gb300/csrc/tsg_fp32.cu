@@ -306,8 +306,9 @@ __global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float
 // matrix sum_j m_Vj (-dx_j) (grad W_j)^T is symmetric (grad W is parallel to dx), so it
 // and its inverse are held as six planes (xx, yy, zz, xy, xz, yz); m holds them too.
 template <int DIM>
-__device__ __forceinline__ void inv_store(const K32& k, float* L, int i, const float* m, bool flow_i) {
-    float inv[6] = {1.f, 1.f, 1.f, 0.f, 0.f, 0.f};
+__device__ __forceinline__ void inv6(const float* m, bool flow_i, float* inv) {
+    inv[0] = inv[1] = inv[2] = 1.f;
+    inv[3] = inv[4] = inv[5] = 0.f;
     if (flow_i) {
         const float xx = m[0], yy = m[1], zz = m[2], xy = m[3], xz = m[4], yz = m[5];
         if (DIM == 2) {
@@ -327,6 +328,11 @@ __device__ __forceinline__ void inv_store(const K32& k, float* L, int i, const f
             }
         }
     }
+}
+template <int DIM>
+__device__ __forceinline__ void inv_store(const K32& k, float* L, int i, const float* m, bool flow_i) {
+    float inv[6];
+    inv6<DIM>(m, flow_i, inv);
     for (int q = 0; q < 6; ++q) L[(size_t)q * k.n + i] = inv[q];
 }
 
@@ -338,35 +344,48 @@ __device__ __forceinline__ void load_L(const float* __restrict__ L6, size_t n, i
         for (int b = 0; b < 3; ++b) L[3 * a + b] = l[sym_idx(a, b)];
 }
 
+// One neighbour's terms of the CSPM sums, shared by the correction kernel and the fused
+// first rates pass so that both give the same bits: the Shepard sum over flow neighbours
+// and the six planes of sum_j m_Vj (-dx_j) (G_j m_Vj dx_j)^T over same-type neighbours.
+template <int DIM>
+__device__ __forceinline__ void cspm_terms(CSum& s, float* L, const float* d, float w, float g, float mVj,
+                                           bool flow_j, bool want_L) {
+    if (flow_j) s.p = __fmaf_rn(mVj, w, s.p);
+    if (want_L) {
+        const float gf = __fmul_rn(g, mVj);
+        for (int a = 0; a < DIM; ++a)
+            for (int b = a; b < DIM; ++b) L[sym_idx(a, b)] = __fmaf_rn(-d[a], __fmul_rn(gf, d[b]), L[sym_idx(a, b)]);
+    }
+}
+
 // CSPM (eng/solver_sph_base.py:386-423).
 template <int DIM, bool FB, int KT>
-// Main pass: the dynamic block, then the static-block particles with a non-empty list
-// (act[0 .. *nact)); the others keep the values written at the list build.
+// Main pass: the dynamic block up to lim, then the static-block particles with a non-empty
+// list (act[0 .. *nact)); the others keep the values written at the list build.
+// skip_fluid: the fluid's factors are computed by the first rates pass of the step (the
+// leap-frog step sequence), so fluid particles are passed over.
 __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                          const int* __restrict__ sstart, const int* __restrict__ act, const int* __restrict__ nact,
-                         Ovf ovf) {
-    FOR_PARTICLES_ACT(FB, 0, k.nd, act, nact, k.n, ovf, t.cnt, k.maxn, {
+                         int lim, int skip_fluid, Ovf ovf) {
+    FOR_PARTICLES_ACT(FB, 0, lim, act, nact, k.n, ovf, t.cnt, k.maxn, {
         const int ti = tf_type(p.hi[i].w);
-        const bool flow_i = is_flow(ti);
-        const bool want_L = k.corr == 1 && flow_i;
-        CSum s;
-        float L[6] = {0, 0, 0, 0, 0, 0};
-        const int ci = type_class(ti);
-        for_nbrs_g<DIM, FB, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, flow_i,
-                                  [](int) { return NoPayload{}; },
-                                  [&](int, const float* d, float r2, int sidx, int cj, float mVj, NoPayload) {
-            const WG wg = w_pair<true, true, KT>(k, r2);
-            if (code_flow(cj)) s.add(mVj * wg.w);
-            if (sidx % kFlushEvery == kFlushEvery - 1) s.flush();
-            if (want_L && cj == ci) {
-                const float gf = wg.g * mVj;
-                for (int a = 0; a < DIM; ++a)
-                    for (int b = a; b < DIM; ++b) L[sym_idx(a, b)] += (-d[a]) * (gf * d[b]);
-            }
-        });
-        const float sum = s.get();
-        t.cf[i] = sum != 0.f ? 1.f / sum : 1.f;
-        if (k.corr == 1) inv_store<DIM>(k, t.L, i, L, want_L);
+        if (!(skip_fluid && ti == MAT_FLUID)) {
+            const bool flow_i = is_flow(ti);
+            const bool want_L = k.corr == 1 && flow_i;
+            CSum s;
+            float L[6] = {0, 0, 0, 0, 0, 0};
+            const int ci = type_class(ti);
+            for_nbrs_g<DIM, FB, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, flow_i,
+                                      [](int) { return NoPayload{}; },
+                                      [&](int, const float* d, float r2, int sidx, int cj, float mVj, NoPayload) {
+                const WG wg = w_pair<true, true, KT>(k, r2);
+                cspm_terms<DIM>(s, L, d, wg.w, wg.g, mVj, code_flow(cj), want_L && cj == ci);
+                if (sidx % kFlushEvery == kFlushEvery - 1) s.flush();
+            });
+            const float sum = s.get();
+            t.cf[i] = sum != 0.f ? 1.f / sum : 1.f;
+            if (k.corr == 1) inv_store<DIM>(k, t.L, i, L, want_L);
+        }
     });
 }
 
@@ -472,9 +491,16 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
 // WCSPH continuity + momentum (eng/solver_sph_wc.py:108-126).
 // KT: kernel function (w_pair); REP: repulsive boundary forces on (1), off (0) or chosen at
 // run time from k.boundary (-1).
-template <int DIM, bool FB, bool CORR, int KT, int REP>
-__global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
+// FL (with CORR): the fluid's CSPM factors are computed here, in the same neighbour loop,
+// instead of by the correction kernel (the first rates pass of a leap-frog step: the
+// particles do not move between the correction and the second pass, which reads them back).
+// The continuity sum then runs on the symmetric part of sum_j m_Vj G_j (v_i - v_j) dx_j^T,
+// contracted with the inverse CSPM matrix once the loop has built it:
+// (L (v_i - v_j)) . dx = sum_ab L_ab dv_b dx_a and L is symmetric.
+template <int DIM, bool FB, bool CORR, int KT, int REP, bool FL = false>
+__global__ void __launch_bounds__(256, FL ? 3 : 4) k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                           const int* __restrict__ sstart, Ovf ovf) {
+    static_assert(!FL || CORR, "the fused CSPM pass needs the correction");
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
       const float wi = p.hi[i].w;
       if (tf_type(wi) == MAT_FLUID) {
@@ -483,9 +509,12 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         const float rti = k.rho0 + t.drt[i];
         const float visc_b = k.rho0 / rti;
         float L[9];
-        if (CORR)
+        if (CORR && !FL)
             load_L(t.L, k.n, i, L);
         CSum dd, dv[3];
+        CSum sh;                                 // FL: Shepard sum
+        float A[6] = {0, 0, 0, 0, 0, 0};         // FL: continuity tensor (symmetric part)
+        float M[6] = {0, 0, 0, 0, 0, 0};         // FL: CSPM matrix
         const bool rep_on = REP < 0 ? (k.boundary == 3 || k.boundary == 4) : REP == 1;
         // viscosity factor for fluid and for boundary neighbours; -rho0 p_i / rho_i^2
         const float vf_f = visc_fac, vf_b = visc_fac * visc_b;
@@ -493,20 +522,30 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         for_nbrs_g<DIM, FB, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
                                   [&](int j) { return __ldg(t.vt + j); },
                                   [&](int, const float* d, float r2, int sidx, int cj, float mVj, const float4& vtj) {
-            const WG wg = w_pair<false, true, KT>(k, r2);
+            const WG wg = w_pair<FL, true, KT>(k, r2);
             const float r = wg.r;
             const float mg = mVj * wg.g;   // m_Vj G, grad W = G d
             const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = DIM == 3 ? vti.z - vtj.z : 0.f;
             const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
-            // continuity: m_Vj (v_i - v_j) . (L_i grad W) = m_Vj G (L_i (v_i - v_j)) . d (L_i symmetric)
-            float cdx = vdx;
-            if (CORR) {
-                const float ux = L[0] * dvx + L[1] * dvy + (DIM == 3 ? L[2] * dvz : 0.f);
-                const float uy = L[3] * dvx + L[4] * dvy + (DIM == 3 ? L[5] * dvz : 0.f);
-                const float uz = DIM == 3 ? L[6] * dvx + L[7] * dvy + L[8] * dvz : 0.f;
-                cdx = ux * d[0] + uy * d[1] + (DIM == 3 ? uz * d[2] : 0.f);
+            if (FL) {
+                cspm_terms<DIM>(sh, M, d, wg.w, wg.g, mVj, code_flow(cj), cj == kCodeFluid);
+                const float dvv[3] = {dvx, dvy, dvz};
+                for (int a = 0; a < DIM; ++a) {
+                    const float ma = mg * dvv[a];
+                    A[a] = fmaf(ma, d[a], A[a]);
+                    for (int b = a + 1; b < DIM; ++b) A[sym_idx(a, b)] = fmaf(ma, d[b], fmaf(mg * dvv[b], d[a], A[sym_idx(a, b)]));
+                }
+            } else {
+                // continuity: m_Vj (v_i - v_j) . (L_i grad W) = m_Vj G (L_i (v_i - v_j)) . d (L_i symmetric)
+                float cdx = vdx;
+                if (CORR) {
+                    const float ux = L[0] * dvx + L[1] * dvy + (DIM == 3 ? L[2] * dvz : 0.f);
+                    const float uy = L[3] * dvx + L[4] * dvy + (DIM == 3 ? L[5] * dvz : 0.f);
+                    const float uz = DIM == 3 ? L[6] * dvx + L[7] * dvy + L[8] * dvz : 0.f;
+                    cdx = ux * d[0] + uy * d[1] + (DIM == 3 ? uz * d[2] : 0.f);
+                }
+                dd.add(mg * cdx);
             }
-            dd.add(mg * cdx);
             // viscosity (fluid or boundary neighbours) and pressure, on the uncorrected gradient.
             // WCSPH scenes hold fluid, dummy, repulsive and rigid particles only (soil is rejected
             // at upload), so every non-fluid neighbour takes the boundary form
@@ -526,9 +565,26 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
             dv[0].add(sc * d[0]);
             dv[1].add(sc * d[1]);
             if (DIM == 3) dv[2].add(sc * d[2]);
-            if (sidx % kFlushEvery == kFlushEvery - 1) { dd.flush(); dv[0].flush(); dv[1].flush(); dv[2].flush(); }
+            if (sidx % kFlushEvery == kFlushEvery - 1) {
+                if (FL) sh.flush();
+                else dd.flush();
+                dv[0].flush(); dv[1].flush(); dv[2].flush();
+            }
         });
-        t.dd[i] = dd.get() * rti;
+        float ddi;
+        if (FL) {
+            const float sum = sh.get();
+            t.cf[i] = sum != 0.f ? 1.f / sum : 1.f;
+            float inv[6];
+            inv6<DIM>(M, true, inv);
+            for (int q = 0; q < 6; ++q) t.L[(size_t)q * k.n + i] = inv[q];
+            ddi = 0.f;
+            for (int a = 0; a < DIM; ++a)
+                for (int b = a; b < DIM; ++b) ddi = fmaf(inv[sym_idx(a, b)], A[sym_idx(a, b)], ddi);
+        } else {
+            ddi = dd.get();
+        }
+        t.dd[i] = ddi * rti;
         t.dv[i] = make_float4(dv[0].get() + k.g[0], dv[1].get() + k.g[1],
                               (DIM == 3 ? dv[2].get() : 0.f) + k.g[2], 0.f);
       }
@@ -1867,16 +1923,23 @@ bool fp32_rebuild_due(Fp32State& st, cudaStream_t s) {
 // repulsive-boundary mode); their overflow pass (a few particles) decides both at run time.
 // Grids of the main passes cover the largest possible count of listed static particles;
 // the threads past the device count return at once.
+// skip_fluid: the first rates pass computes the fluid's factors; when the dynamic block holds
+// fluid only, the main pass then visits the listed static particles alone.
 template <int DIM>
-void corr_launch(Fp32State& st, cudaStream_t s, const Ovf& ovf) {
+void corr_launch(Fp32State& st, cudaStream_t s, const Ovf& ovf, bool skip_fluid) {
     const K32& k = st.k;
     const P32& p = st.P[st.cur];
-    const int nb = nblk(k.n, st.tpb);
+    const int lim = skip_fluid && st.c.n_bdy <= k.n - k.nd ? 0 : k.nd;
+    const int nb = nblk(lim + (k.n - k.nd), st.tpb);
+    const int sf = skip_fluid ? 1 : 0;
     if (k.kernel == 1)
-        TSG_LAUNCH((k_corr32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact, ovf);
+        TSG_LAUNCH((k_corr32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact,
+                   lim, sf, ovf);
     else
-        TSG_LAUNCH((k_corr32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact, ovf);
-    TSG_LAUNCH((k_corr32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact, ovf);
+        TSG_LAUNCH((k_corr32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact,
+                   lim, sf, ovf);
+    TSG_LAUNCH((k_corr32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact, lim, sf,
+               ovf);
 }
 
 // WCSPH boundary extrapolation over [base, base + count_n); the static block (base = nd)
@@ -1896,31 +1959,33 @@ void bdy_launch(Fp32State& st, const P32& p, int base, int count_n, cudaStream_t
                st.nsact, ovf);
 }
 
-template <int DIM, bool CORR, int KT>
+template <int DIM, bool CORR, int KT, bool FL>
 void rates_main(Fp32State& st, const P32& p, cudaStream_t s, const Ovf& ovf) {
     const K32& k = st.k;
     const int nb = nblk(k.nd, st.tpb);
     if (k.boundary == 3 || k.boundary == 4)
-        TSG_LAUNCH((k_rates32<DIM, false, CORR, KT, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+        TSG_LAUNCH((k_rates32<DIM, false, CORR, KT, 1, FL>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
     else
-        TSG_LAUNCH((k_rates32<DIM, false, CORR, KT, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+        TSG_LAUNCH((k_rates32<DIM, false, CORR, KT, 0, FL>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
 }
 
-template <int DIM, bool CORR>
+template <int DIM, bool CORR, bool FL = false>
 void rates_launch(Fp32State& st, const P32& p, cudaStream_t s, const Ovf& ovf) {
     const K32& k = st.k;
-    if (k.kernel == 1) rates_main<DIM, CORR, 1>(st, p, s, ovf);
-    else rates_main<DIM, CORR, 0>(st, p, s, ovf);
-    TSG_LAUNCH((k_rates32<DIM, true, CORR, -1, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
+    if (k.kernel == 1) rates_main<DIM, CORR, 1, FL>(st, p, s, ovf);
+    else rates_main<DIM, CORR, 0, FL>(st, p, s, ovf);
+    TSG_LAUNCH((k_rates32<DIM, true, CORR, -1, -1, FL>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
 }
 
-void fp32_kernel_corr(Fp32State& st, cudaStream_t s) {
+static void kernel_corr(Fp32State& st, cudaStream_t s, bool skip_fluid) {
     PhaseScope ph(s, PH_CORR);
     const K32& k = st.k;
     const Ovf ovf{st.ovf_list, st.novf};
-    if (k.dim == 2) corr_launch<2>(st, s, ovf);
-    else corr_launch<3>(st, s, ovf);
+    if (k.dim == 2) corr_launch<2>(st, s, ovf, skip_fluid);
+    else corr_launch<3>(st, s, ovf, skip_fluid);
 }
+
+void fp32_kernel_corr(Fp32State& st, cudaStream_t s) { kernel_corr(st, s, false); }
 
 void fp32_init_tmp(Fp32State& st, cudaStream_t s) {
     PhaseScope ph(s, PH_INIT);
@@ -1969,8 +2034,9 @@ void soil_one_step(Fp32State& st, cudaStream_t s) {
 }
 
 // eos = false: the fluid pressures were computed by the kernel before (the step sequence
-// fuses them into init_real2tmp and the leap-frog half step).
-static void one_step(Fp32State& st, cudaStream_t s, bool eos) {
+// fuses them into init_real2tmp and the leap-frog half step).  fl: the rates pass computes
+// the fluid's CSPM factors (the correction kernel of the step skipped them).
+static void one_step(Fp32State& st, cudaStream_t s, bool eos, bool fl = false) {
     const K32& k = st.k;
     P32& p = st.P[st.cur];
     if (k.solver != 1) {
@@ -1996,7 +2062,10 @@ static void one_step(Fp32State& st, cudaStream_t s, bool eos) {
     {
         PhaseScope ph(s, PH_RATES);
         const Ovf ovf{st.ovf_list, st.novf};
-        if (k.dim == 2) { if (k.corr) rates_launch<2, true>(st, p, s, ovf); else rates_launch<2, false>(st, p, s, ovf); }
+        if (fl) {
+            if (k.dim == 2) rates_launch<2, true, true>(st, p, s, ovf);
+            else rates_launch<3, true, true>(st, p, s, ovf);
+        } else if (k.dim == 2) { if (k.corr) rates_launch<2, true>(st, p, s, ovf); else rates_launch<2, false>(st, p, s, ovf); }
         else { if (k.corr) rates_launch<3, true>(st, p, s, ovf); else rates_launch<3, false>(st, p, s, ovf); }
     }
 }
@@ -2059,10 +2128,13 @@ void fp32_rk_update(Fp32State& st, int m, cudaStream_t s) {
 // the integrator's one_step / advect sequence, advect_pos, advect_something and, in
 // collision mode, enforce_boundary (eng/solver_sph_base.py:41-61, :79-120).
 void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
-    fp32_kernel_corr(st, s);
     // WCSPH with symplectic Euler or leap-frog: the fluid EOS (first phase of each one_step)
     // runs inside init_real2tmp and the half step, which produce its input density_tmp
     const bool fuse = st.k.solver == 1 && st.c.ti != 4;
+    // WCSPH leap-frog with CSPM: the fluid's CSPM factors come from the first rates pass
+    // (positions stay fixed through both one_steps, so the second pass reads them back)
+    const bool fuse_corr = fuse && st.c.ti == 2 && st.k.corr == 1;
+    kernel_corr(st, s, fuse_corr);
     if (fuse) {
         PhaseScope ph(s, PH_INIT);
         TSG_LAUNCH(k_init_tmp32<true>, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T);
@@ -2079,7 +2151,7 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
         }
         fp32_advect(st, TSG_RK_FINAL, s);
     } else {
-        one_step(st, s, !fuse);
+        one_step(st, s, !fuse, fuse_corr);
         if (st.c.ti == 2) {
             if (fuse) {
                 PhaseScope ph(s, PH_INTEGRATE);

@@ -160,15 +160,16 @@ template <bool VAL, bool GRAD, int KT = -1>
 __device__ __forceinline__ WG w_pair(const K32& k, float r2) {
     const float rs = rsqrtf(r2);
     WG o;
-    o.r = r2 * rs;
+    o.r = __fmul_rn(r2, rs);
     o.w = 0.f;
     o.g = 0.f;
     if (!(o.r > 1e-8f)) return o;
-    const float q = o.r * k.h1;
+    const float q = __fmul_rn(o.r, k.h1);
     if (KT == 1 || (KT < 0 && k.kernel == 1)) {
-        const float q1 = 1.f - 0.5f * q, q2 = q1 * q1;
-        if (VAL) o.w = k.kk * (q2 * q2) * (1.f + 2.f * q);
-        if (GRAD) o.g = k.wgrad * (q2 * q1);
+        // rounding spelled out, so every kernel that inlines this gets the same bits
+        const float q1 = __fmaf_rn(-0.5f, q, 1.f), q2 = __fmul_rn(q1, q1);
+        if (VAL) o.w = __fmul_rn(__fmul_rn(k.kk, __fmul_rn(q2, q2)), __fmaf_rn(2.f, q, 1.f));
+        if (GRAD) o.g = __fmul_rn(k.wgrad, __fmul_rn(q2, q1));
         return o;
     }
     const float t = 2.f - q;
