@@ -178,7 +178,7 @@ def cpu_baseline(cfg_dict, budget_s=25.0):
 
 
 # ---------------------------------------------------------------- GPU measurement
-def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None):
+def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None, fused_corr=False):
     """Unique bytes a kernel must move once per launch (neighbour re-reads excluded).
 
     Every per-particle array the kernel touches counts once (read or written), as does
@@ -199,6 +199,10 @@ def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None):
               CSPM_f (4) and the writes (v_tmp, p / rho^2) (16), (p, rho) (8),
               density_tmp (4), pressure (4); per flow particle lo + v_tmp + (p, rho)
               (16 + 16 + 8); plus the dummies' list entries.
+    fused_corr (FP32-mixed leap-frog with CSPM: the first rates pass computes the flow
+    particles' CSPM factors): the rates figure is the mean of the two passes, the first
+    writing CSPM_f (4) and CSPM_L (24) instead of reading CSPM_L (24), so 26 B per flow
+    particle; the correction kernel visits the listed dummies only.
     """
     if precision == "fp64":
         if kernel != "rates":
@@ -209,8 +213,11 @@ def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None):
     na = lists.get("listed_dummies", n_total - n_flow)
     n_vis = n_flow + na
     if kernel == "rates":
-        return n_vis * 32 + n_flow * (16 + 4 + 4 + (24 if corr else 0) + 20) + 4 * er
+        cspm = (26 if fused_corr else 24) if corr else 0
+        return n_vis * 32 + n_flow * (16 + 4 + 4 + cspm + 20) + 4 * er
     if kernel == "kernel_corr":
+        if fused_corr:
+            return na * (36 + 4 + 24 + 4) + 4 * ed
         return n_vis * (36 + 4 + (24 if corr else 0)) + na * 4 + 4 * (er + ed)
     if kernel == "boundary":
         return na * (4 + 48 + 4 + 4 + 32) + n_flow * 40 + 4 * ed
@@ -416,7 +423,9 @@ def run_ours(args):
     n_flow = h["n_fluid"]
     def roof(kernel):
         ph = h["phases"].get(kernel)
-        alg = algorithmic_bytes(kernel, h["n_total"], n_flow, head, corr, h.get("lists"))
+        fused = head == "fp32_mixed" and corr and cfg_dict["Configuration"].get("timeIntegration") == 2 \
+            and cfg_dict["Configuration"].get("simulationMethod", 1) == 1
+        alg = algorithmic_bytes(kernel, h["n_total"], n_flow, head, corr, h.get("lists"), fused)
         if not ph or not alg or not ph["ms_per_launch"]:
             return None
         ach = alg / (ph["ms_per_launch"] * 1e-3) / 1e9

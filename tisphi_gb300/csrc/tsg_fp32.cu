@@ -24,7 +24,11 @@
 // by the per-step kernels.
 //
 // Sums over neighbours are block-compensated: plain f32 sums over 16 neighbours, then a
-// Kahan update of the running total.
+// Kahan update of the running total.  One exception: in a leap-frog WCSPH step with CSPM
+// the first rates pass also builds the fluid's CSPM factors, so its continuity sum runs
+// as a plain f32 tensor contracted with the inverse matrix after the loop; it sets only
+// the half-step density, while the step's density update takes the second pass's
+// compensated sum.
 //
 // Reference: eng/particle_system.py:228-269 (cell list), eng/solver_sph_base.py:41-238,
 // :363-423, :648-669 (step, CSPM, boundary), eng/solver_sph_wc.py:82-132 (WCSPH).
@@ -347,15 +351,14 @@ __device__ __forceinline__ void load_L(const float* __restrict__ L6, size_t n, i
 // One neighbour's terms of the CSPM sums, shared by the correction kernel and the fused
 // first rates pass so that both give the same bits: the Shepard sum over flow neighbours
 // and the six planes of sum_j m_Vj (-dx_j) (G_j m_Vj dx_j)^T over same-type neighbours.
+// e = G_j m_Vj dx_j (the corrected kernel gradient's input, e_b = __fmul_rn(G m_V, dx_b)).
 template <int DIM>
-__device__ __forceinline__ void cspm_terms(CSum& s, float* L, const float* d, float w, float g, float mVj,
+__device__ __forceinline__ void cspm_terms(CSum& s, float* L, const float* d, const float* e, float w, float mVj,
                                            bool flow_j, bool want_L) {
     if (flow_j) s.p = __fmaf_rn(mVj, w, s.p);
-    if (want_L) {
-        const float gf = __fmul_rn(g, mVj);
+    if (want_L)
         for (int a = 0; a < DIM; ++a)
-            for (int b = a; b < DIM; ++b) L[sym_idx(a, b)] = __fmaf_rn(-d[a], __fmul_rn(gf, d[b]), L[sym_idx(a, b)]);
-    }
+            for (int b = a; b < DIM; ++b) L[sym_idx(a, b)] = __fmaf_rn(-d[a], e[b], L[sym_idx(a, b)]);
 }
 
 // CSPM (eng/solver_sph_base.py:386-423).
@@ -379,7 +382,9 @@ __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const fl
                                       [](int) { return NoPayload{}; },
                                       [&](int, const float* d, float r2, int sidx, int cj, float mVj, NoPayload) {
                 const WG wg = w_pair<true, true, KT>(k, r2);
-                cspm_terms<DIM>(s, L, d, wg.w, wg.g, mVj, code_flow(cj), want_L && cj == ci);
+                const float gf = __fmul_rn(wg.g, mVj);
+                const float e[3] = {__fmul_rn(gf, d[0]), __fmul_rn(gf, d[1]), __fmul_rn(gf, d[2])};
+                cspm_terms<DIM>(s, L, d, e, wg.w, mVj, code_flow(cj), want_L && cj == ci);
                 if (sidx % kFlushEvery == kFlushEvery - 1) s.flush();
             });
             const float sum = s.get();
@@ -498,7 +503,7 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
 // contracted with the inverse CSPM matrix once the loop has built it:
 // (L (v_i - v_j)) . dx = sum_ab L_ab dv_b dx_a and L is symmetric.
 template <int DIM, bool FB, bool CORR, int KT, int REP, bool FL = false>
-__global__ void __launch_bounds__(256, FL ? 3 : 4) k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
+__global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                           const int* __restrict__ sstart, Ovf ovf) {
     static_assert(!FL || CORR, "the fused CSPM pass needs the correction");
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
@@ -524,16 +529,18 @@ __global__ void __launch_bounds__(256, FL ? 3 : 4) k_rates32(K32 k, P32 p, T32 t
                                   [&](int, const float* d, float r2, int sidx, int cj, float mVj, const float4& vtj) {
             const WG wg = w_pair<FL, true, KT>(k, r2);
             const float r = wg.r;
-            const float mg = mVj * wg.g;   // m_Vj G, grad W = G d
+            const float mg = __fmul_rn(wg.g, mVj);   // m_Vj G, grad W = G d
             const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = DIM == 3 ? vti.z - vtj.z : 0.f;
             const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
             if (FL) {
-                cspm_terms<DIM>(sh, M, d, wg.w, wg.g, mVj, code_flow(cj), cj == kCodeFluid);
+                // WCSPH scenes hold no soil: the flow neighbours are the fluid ones
+                const float e[3] = {__fmul_rn(mg, d[0]), __fmul_rn(mg, d[1]), __fmul_rn(mg, d[2])};
+                const bool fj = cj == kCodeFluid;
+                cspm_terms<DIM>(sh, M, d, e, wg.w, mVj, fj, fj);
                 const float dvv[3] = {dvx, dvy, dvz};
                 for (int a = 0; a < DIM; ++a) {
-                    const float ma = mg * dvv[a];
-                    A[a] = fmaf(ma, d[a], A[a]);
-                    for (int b = a + 1; b < DIM; ++b) A[sym_idx(a, b)] = fmaf(ma, d[b], fmaf(mg * dvv[b], d[a], A[sym_idx(a, b)]));
+                    A[a] = fmaf(dvv[a], e[a], A[a]);
+                    for (int b = a + 1; b < DIM; ++b) A[sym_idx(a, b)] = fmaf(dvv[a], e[b], fmaf(dvv[b], e[a], A[sym_idx(a, b)]));
                 }
             } else {
                 // continuity: m_Vj (v_i - v_j) . (L_i grad W) = m_Vj G (L_i (v_i - v_j)) . d (L_i symmetric)
