@@ -69,7 +69,7 @@ struct Pair {
 __device__ __forceinline__ bool pair(const K32& k, const Start& S, int a, int b, Pair& P) {
     float d[3];
     delta<2>(S.hi[a], S.lo[a], S.hi[b], S.lo[b], d);
-    const float r2 = d[0] * d[0] + d[1] * d[1];
+    const float r2 = dist2<2>(d);
     if (!(r2 < k.R2)) return false;
     P.dx = d[0];
     P.dy = d[1];
@@ -203,7 +203,7 @@ __global__ void k_adj_bdy(K32 k, P32 p, T32 t, Start S, A32 A) {
     for_list(k, t, b, [&](int j) {
         float d[3];
         delta<2>(S.hi[b], S.lo[b], S.hi[j], S.lo[j], d);
-        const float r2 = d[0] * d[0] + d[1] * d[1];
+        const float r2 = dist2<2>(d);
         if (!(r2 < k.R2) || !soil(S.hi[j].w)) return;
         const float mw = S.lo[j].w * w_val(k, fast_sqrt(r2));
         const float4 v = S.vel[j];
@@ -248,7 +248,7 @@ __global__ void k_adj_bdy_soil(K32 k, P32 p, T32 t, Start S, A32 A) {
         if (tf_type(S.hi[b].w) > 0) return;
         float d[3];
         delta<2>(S.hi[b], S.lo[b], S.hi[j], S.lo[j], d);  // d_bj = x_b - x_j
-        const float r2 = d[0] * d[0] + d[1] * d[1];
+        const float r2 = dist2<2>(d);
         if (!(r2 < k.R2)) return;
         const float r = fast_sqrt(r2);
         const float W = w_val(k, r), G = w_grad(k, r);
@@ -615,7 +615,7 @@ __global__ void k_wadj_bdy(K32 k, P32 p, T32 t, Start S, A32 A) {
         if (!fluid(S.hi[j].w)) return;
         float d[3];
         delta<2>(S.hi[b], S.lo[b], S.hi[j], S.lo[j], d);
-        const float r2 = d[0] * d[0] + d[1] * d[1];
+        const float r2 = dist2<2>(d);
         if (!(r2 < k.R2)) return;
         const float mw = S.lo[j].w * w_val(k, fast_sqrt(r2));
         const float4 v = t.vt[j];
@@ -648,7 +648,7 @@ __global__ void k_wadj_bdy_fluid(K32 k, P32 p, T32 t, Start S, A32 A) {
         if (tf_type(S.hi[b].w) > 0) return;
         float d[3];
         delta<2>(S.hi[b], S.lo[b], S.hi[j], S.lo[j], d);  // d = x_b - x_j
-        const float r2 = d[0] * d[0] + d[1] * d[1];
+        const float r2 = dist2<2>(d);
         if (!(r2 < k.R2)) return;
         const float r = fast_sqrt(r2);
         const float W = w_val(k, r), G = w_grad(k, r);

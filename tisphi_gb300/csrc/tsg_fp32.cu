@@ -456,7 +456,11 @@ __global__ void k_pre32(K32 k, P32 p, T32 t) {
 }
 
 // Boundary extrapolation for dummy / repulsive / rigid particles in [base, base + count_n) (WC).
-template <int DIM, bool FB, int KT>
+// SH: the particle's Shepard factor is summed in the same loop (its list holds flow
+// neighbours only, in the correction kernel's order, so the factor has the same bits) and
+// stored, instead of read (the first one_step of a leap-frog WCSPH step with CSPM, whose
+// correction kernel then has nothing left to visit in the static block).
+template <int DIM, bool FB, int KT, bool SH = false>
 __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                         const int* __restrict__ sstart, int base, int count_n, const int* __restrict__ act,
                         const int* __restrict__ nact, Ovf ovf) {
@@ -465,22 +469,31 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
     FOR_PARTICLES_ACT(FB, base, act ? base : lim, act, nact, lim, ovf, t.cnt, k.maxn, {
         const int ti = tf_type(p.hi[i].w);
         if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
-            CSum bv[3], bp;
-            const float4 hi_i = p.hi[i], lo_i = p.lo[i];
+            CSum bv[3], bp, sh;
             for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
                               [&](int j, const float* d, float r2, int sidx, int, float mV) {
                 const float w = w_pair<true, false, KT>(k, r2).w;
                 const float4 vt = t.vt[j];
                 const float2 pr = t.pr[j];
                 const float mw = mV * w;
+                if (SH) sh.p = __fmaf_rn(mV, w, sh.p);
                 bv[0].add(mw * vt.x);
                 bv[1].add(mw * vt.y);
                 if (DIM == 3) bv[2].add(mw * vt.z);
                 bp.add(mw * (pr.x + pr.y * k.g[1] * d[1]));
-                if (sidx % kFlushEvery == kFlushEvery - 1) { bv[0].flush(); bv[1].flush(); bv[2].flush(); bp.flush(); }
+                if (sidx % kFlushEvery == kFlushEvery - 1) {
+                    bv[0].flush(); bv[1].flush(); bv[2].flush(); bp.flush();
+                    if (SH) sh.flush();
+                }
             });
-            (void)hi_i; (void)lo_i;
-            const float f = t.cf[i];
+            float f;
+            if (SH) {
+                const float sum = sh.get();
+                f = sum != 0.f ? 1.f / sum : 1.f;
+                t.cf[i] = f;
+            } else {
+                f = t.cf[i];
+            }
             const float4 v = p.vel[i];
             const float pv = fmaxf(bp.get() * f, 0.f);
             const float b0 = bv[0].get(), b1 = bv[1].get(), b2 = DIM == 3 ? bv[2].get() : 0.f;
@@ -1366,7 +1379,7 @@ __global__ void k_nbr_count_ell(K32 k, const float4* HI, const float4* LO, const
         const int j = entry_index(k, nbr[(size_t)q * k.n + i]);
         float d[3];
         delta<DIM>(HI[i], LO[i], HI[j], LO[j], d);
-        const float r2 = d[0] * d[0] + d[1] * d[1] + (DIM == 3 ? d[2] * d[2] : 0.f);
+        const float r2 = dist2<DIM>(d);
         if (r2 < k.R2) ++c;
     }
     counts[i] = c;
@@ -1384,7 +1397,7 @@ __global__ void k_nbr_fill_ell(K32 k, const float4* HI, const float4* LO, const 
             const int j = entry_index(k, nbr[(size_t)q * k.n + i]);
             float d[3];
             delta<DIM>(HI[i], LO[i], HI[j], LO[j], d);
-            const float r2 = d[0] * d[0] + d[1] * d[1] + (DIM == 3 ? d[2] * d[2] : 0.f);
+            const float r2 = dist2<DIM>(d);
             if (r2 < k.R2) list[w++] = j;
         }
     } else {
@@ -1818,12 +1831,13 @@ __global__ void k_static_active(K32 k, P32 p, T32 t, int wc, int* __restrict__ a
     if (lane == 0 && ball) base = atomicAdd(nact, __popc(ball));
     base = __shfl_sync(0xffffffffu, base, 0);
     if (on) act[base + __popc(ball & ((1u << lane) - 1u))] = i;
-    if (!in || on) return;
-    t.cf[i] = 1.f;
-    if (t.L) {
+    if (!in) return;
+    if (t.L) {  // no static particle is a flow particle: its CSPM matrix is the identity
         const size_t n = k.n;
         for (int q = 0; q < 6; ++q) t.L[q * n + i] = q < 3 ? 1.f : 0.f;
     }
+    if (on) return;
+    t.cf[i] = 1.f;
     if (!wc) return;
     const int ti = tf_type(p.hi[i].w);
     if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
@@ -1951,18 +1965,18 @@ void corr_launch(Fp32State& st, cudaStream_t s, const Ovf& ovf, bool skip_fluid)
 
 // WCSPH boundary extrapolation over [base, base + count_n); the static block (base = nd)
 // visits its listed particles only.
-template <int DIM>
+template <int DIM, bool SH>
 void bdy_launch(Fp32State& st, const P32& p, int base, int count_n, cudaStream_t s, const Ovf& ovf) {
     const K32& k = st.k;
     const int nb = nblk(count_n, st.tpb);
     const int* act = base == k.nd ? st.sact : nullptr;
     if (k.kernel == 1)
-        TSG_LAUNCH((k_bdy32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, act,
-                   st.nsact, ovf);
+        TSG_LAUNCH((k_bdy32<DIM, false, 1, SH>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n,
+                   act, st.nsact, ovf);
     else
-        TSG_LAUNCH((k_bdy32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, act,
-                   st.nsact, ovf);
-    TSG_LAUNCH((k_bdy32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, act,
+        TSG_LAUNCH((k_bdy32<DIM, false, 0, SH>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n,
+                   act, st.nsact, ovf);
+    TSG_LAUNCH((k_bdy32<DIM, true, -1, SH>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, base, count_n, act,
                st.nsact, ovf);
 }
 
@@ -2042,8 +2056,9 @@ void soil_one_step(Fp32State& st, cudaStream_t s) {
 
 // eos = false: the fluid pressures were computed by the kernel before (the step sequence
 // fuses them into init_real2tmp and the leap-frog half step).  fl: the rates pass computes
-// the fluid's CSPM factors (the correction kernel of the step skipped them).
-static void one_step(Fp32State& st, cudaStream_t s, bool eos, bool fl = false) {
+// the fluid's CSPM factors (the correction kernel of the step skipped them); sh: the
+// boundary pass computes the static block's Shepard factors (no correction kernel ran).
+static void one_step(Fp32State& st, cudaStream_t s, bool eos, bool fl = false, bool sh = false) {
     const K32& k = st.k;
     P32& p = st.P[st.cur];
     if (k.solver != 1) {
@@ -2058,13 +2073,18 @@ static void one_step(Fp32State& st, cudaStream_t s, bool eos, bool fl = false) {
     {
         PhaseScope ph(s, PH_BDY);
         const Ovf ovf{st.ovf_list, st.novf};
-        auto bdy = [&](int base, int count_n) {
+        auto bdy = [&](int base, int count_n, bool shep) {
             if (count_n <= 0) return;
-            if (k.dim == 2) bdy_launch<2>(st, p, base, count_n, s, ovf);
-            else bdy_launch<3>(st, p, base, count_n, s, ovf);
+            if (shep) {
+                if (k.dim == 2) bdy_launch<2, true>(st, p, base, count_n, s, ovf);
+                else bdy_launch<3, true>(st, p, base, count_n, s, ovf);
+            } else {
+                if (k.dim == 2) bdy_launch<2, false>(st, p, base, count_n, s, ovf);
+                else bdy_launch<3, false>(st, p, base, count_n, s, ovf);
+            }
         };
-        bdy(k.nd, k.n - k.nd);
-        if (st.c.n_bdy > k.n - k.nd) bdy(0, k.nd);  // kinematic rigid particles live in the dynamic block
+        bdy(k.nd, k.n - k.nd, sh);
+        if (st.c.n_bdy > k.n - k.nd) bdy(0, k.nd, false);  // kinematic rigid particles live in the dynamic block
     }
     {
         PhaseScope ph(s, PH_RATES);
@@ -2141,7 +2161,10 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
     // WCSPH leap-frog with CSPM: the fluid's CSPM factors come from the first rates pass
     // (positions stay fixed through both one_steps, so the second pass reads them back)
     const bool fuse_corr = fuse && st.c.ti == 2 && st.k.corr == 1;
-    kernel_corr(st, s, fuse_corr);
+    // ... and when the dynamic block holds fluid only, the static block's Shepard factors
+    // come from the first boundary pass, which leaves the correction kernel nothing to do
+    const bool fuse_shep = fuse_corr && st.c.n_bdy <= st.k.n - st.k.nd;
+    if (!fuse_shep) kernel_corr(st, s, fuse_corr);
     if (fuse) {
         PhaseScope ph(s, PH_INIT);
         TSG_LAUNCH(k_init_tmp32<true>, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T);
@@ -2158,7 +2181,7 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
         }
         fp32_advect(st, TSG_RK_FINAL, s);
     } else {
-        one_step(st, s, !fuse, fuse_corr);
+        one_step(st, s, !fuse, fuse_corr, fuse_shep);
         if (st.c.ti == 2) {
             if (fuse) {
                 PhaseScope ph(s, PH_INTEGRATE);

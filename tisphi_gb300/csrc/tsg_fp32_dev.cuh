@@ -182,6 +182,14 @@ __device__ __forceinline__ WG w_pair(const K32& k, float r2) {
     }
     return o;
 }
+// |d|^2 with its rounding spelled out, so that every kernel takes the support test and
+// evaluates the kernel function on the same bits for the same pair.
+template <int DIM>
+__device__ __forceinline__ float dist2(const float* d) {
+    float r2 = __fmaf_rn(d[1], d[1], __fmul_rn(d[0], d[0]));
+    if (DIM == 3) r2 = __fmaf_rn(d[2], d[2], r2);
+    return r2;
+}
 template <int DIM>
 __device__ __forceinline__ void delta(const float4& hi_i, const float4& lo_i, const float4& hi_j, const float4& lo_j,
                                       float* d) {
@@ -238,8 +246,7 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
                     }
                     float d[3];
                     delta<DIM>(hi_i, lo_i, HI[j], LO[j], d);
-                    float r2 = d[0] * d[0] + d[1] * d[1];
-                    if (DIM == 3) r2 += d[2] * d[2];
+                    const float r2 = dist2<DIM>(d);
                     if (!(r2 < cut2)) continue;
                     body(j, d, r2);
                 }
@@ -272,8 +279,7 @@ __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __res
             d[0] = entry_offset(e, 0) * k.Q + (lo_i.x - l.x);
             d[1] = entry_offset(e, 1) * k.Q + (lo_i.y - l.y);
             d[2] = DIM == 3 ? entry_offset(e, 2) * k.Q + (lo_i.z - l.z) : 0.f;
-            float r2 = d[0] * d[0] + d[1] * d[1];
-            if (DIM == 3) r2 += d[2] * d[2];
+            const float r2 = dist2<DIM>(d);
             const int c = (e >> kEntryBits) & 7;
             if (r2 < k.R2) body(e & kEntryMask, d, r2, s, CODE ? c : class_type(c), l.w, g);
         };
