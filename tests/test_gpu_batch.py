@@ -9,9 +9,12 @@
 * Graph replay against the eager step path (per-phase profiling forces eager steps):
   bit-identical, since both launch the same kernels in the same order.
 * The step sequence (fluid EOS inside init_real2tmp and the leap-frog half step; advect,
-  advect_pos and the density clamp in one pass) against the reference's stages called one
-  by one (sort, calc_kernel_corr, init_real2tmp, substep, advect_pos, advect_something),
-  lists rebuilt every step: bit-identical.
+  advect_pos and the density clamp in one pass; Shepard factors from the first rates and
+  boundary passes instead of the correction kernel) against the reference's stages called
+  one by one (sort, calc_kernel_corr, init_real2tmp, substep, advect_pos,
+  advect_something), lists rebuilt every step: bit-identical without CSPM and with CSPM
+  under symplectic Euler (whose single rates pass keeps reading the correction kernel's
+  CSPM matrix).
 * Leap-frog with CSPM, where step() takes the fluid's CSPM factors from the first rates
   pass (the correction kernel then visits the boundary particles only), against the same
   stage calls: the factors bit-identical; the first pass's continuity, contracted with the
@@ -163,9 +166,10 @@ def test_graph_replay_equals_eager(native):
         np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy(), err_msg=nm)
 
 
-@pytest.mark.parametrize("ti", [1, 2])
-def test_step_sequence_equals_stage_calls(native, ti):
-    d = small_dambreak_2d(integration=ti)
+@pytest.mark.parametrize("case", ["2d_se", "2d_lf", "3d_se_cspm"])
+def test_step_sequence_equals_stage_calls(native, case):
+    d = {"2d_se": lambda: small_dambreak_2d(integration=1), "2d_lf": lambda: small_dambreak_2d(integration=2),
+         "3d_se_cspm": lambda: small_dambreak_3d(integration=1)}[case]()
     d["Configuration"]["neighbourSkin"] = 0.0
     a, b = _single(d), _single(d)
     a.solver.step(6)
@@ -176,7 +180,7 @@ def test_step_sequence_equals_stage_calls(native, ti):
         b.solver.substep()
         b.solver.advect_pos()
         b.solver.advect_something()
-    for nm in ("x", "v", "density", "pressure", "id0"):
+    for nm in ("x", "v", "density", "pressure", "id0", "CSPM_f"):
         np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy(), err_msg=nm)
 
 

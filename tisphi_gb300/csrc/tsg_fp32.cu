@@ -364,13 +364,14 @@ __device__ __forceinline__ void cspm_terms(CSum& s, float* L, const float* d, co
 // CSPM (eng/solver_sph_base.py:386-423).
 template <int DIM, bool FB, int KT>
 // Main pass: the dynamic block up to lim, then the static-block particles with a non-empty
-// list (act[0 .. *nact)); the others keep the values written at the list build.
-// skip_fluid: the fluid's factors are computed by the first rates pass of the step (the
-// leap-frog step sequence), so fluid particles are passed over.
+// list (act[0 .. *nact), act may be null); the others keep the values written at the list
+// build.  The overflow pass takes the overflowed particles below nmax.  skip_fluid: the
+// fluid's factors are computed by the first rates pass of the step, so fluid particles are
+// passed over.
 __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                          const int* __restrict__ sstart, const int* __restrict__ act, const int* __restrict__ nact,
-                         int lim, int skip_fluid, Ovf ovf) {
-    FOR_PARTICLES_ACT(FB, 0, lim, act, nact, k.n, ovf, t.cnt, k.maxn, {
+                         int lim, int nmax, int skip_fluid, Ovf ovf) {
+    FOR_PARTICLES_ACT(FB, 0, lim, act, nact, nmax, ovf, t.cnt, k.maxn, {
         const int ti = tf_type(p.hi[i].w);
         if (!(skip_fluid && ti == MAT_FLUID)) {
             const bool flow_i = is_flow(ti);
@@ -509,16 +510,17 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
 // WCSPH continuity + momentum (eng/solver_sph_wc.py:108-126).
 // KT: kernel function (w_pair); REP: repulsive boundary forces on (1), off (0) or chosen at
 // run time from k.boundary (-1).
-// FL (with CORR): the fluid's CSPM factors are computed here, in the same neighbour loop,
-// instead of by the correction kernel (the first rates pass of a leap-frog step: the
-// particles do not move between the correction and the second pass, which reads them back).
-// The continuity sum then runs on the symmetric part of sum_j m_Vj G_j (v_i - v_j) dx_j^T,
-// contracted with the inverse CSPM matrix once the loop has built it:
-// (L (v_i - v_j)) . dx = sum_ab L_ab dv_b dx_a and L is symmetric.
+// FL: the fluid's CSPM factors (the Shepard factor; with CORR the CSPM matrix too) are
+// computed here, in the same neighbour loop, instead of by the correction kernel (the
+// first rates pass of the step: the particles do not move between the correction and the
+// second pass, which reads them back).  With CORR the continuity sum then runs on the
+// symmetric part of sum_j m_Vj G_j (v_i - v_j) dx_j^T, contracted with the inverse CSPM
+// matrix once the loop has built it: (L (v_i - v_j)) . dx = sum_ab L_ab dv_b dx_a and L is
+// symmetric.
 template <int DIM, bool FB, bool CORR, int KT, int REP, bool FL = false>
 __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                           const int* __restrict__ sstart, Ovf ovf) {
-    static_assert(!FL || CORR, "the fused CSPM pass needs the correction");
+    constexpr bool FLC = FL && CORR;  // continuity through the CSPM tensor
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
       const float wi = p.hi[i].w;
       if (tf_type(wi) == MAT_FLUID) {
@@ -545,11 +547,10 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
             const float mg = __fmul_rn(wg.g, mVj);   // m_Vj G, grad W = G d
             const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = DIM == 3 ? vti.z - vtj.z : 0.f;
             const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
-            if (FL) {
-                // WCSPH scenes hold no soil: the flow neighbours are the fluid ones
-                const float e[3] = {__fmul_rn(mg, d[0]), __fmul_rn(mg, d[1]), __fmul_rn(mg, d[2])};
-                const bool fj = cj == kCodeFluid;
-                cspm_terms<DIM>(sh, M, d, e, wg.w, mVj, fj, fj);
+            // WCSPH scenes hold no soil: the flow neighbours are the fluid ones
+            const float e[3] = {__fmul_rn(mg, d[0]), __fmul_rn(mg, d[1]), __fmul_rn(mg, d[2])};
+            if (FL) cspm_terms<DIM>(sh, M, d, e, wg.w, mVj, cj == kCodeFluid, CORR && cj == kCodeFluid);
+            if (FLC) {
                 const float dvv[3] = {dvx, dvy, dvz};
                 for (int a = 0; a < DIM; ++a) {
                     A[a] = fmaf(dvv[a], e[a], A[a]);
@@ -587,14 +588,16 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
             if (DIM == 3) dv[2].add(sc * d[2]);
             if (sidx % kFlushEvery == kFlushEvery - 1) {
                 if (FL) sh.flush();
-                else dd.flush();
+                if (!FLC) dd.flush();
                 dv[0].flush(); dv[1].flush(); dv[2].flush();
             }
         });
-        float ddi;
         if (FL) {
             const float sum = sh.get();
             t.cf[i] = sum != 0.f ? 1.f / sum : 1.f;
+        }
+        float ddi;
+        if (FLC) {
             float inv[6];
             inv6<DIM>(M, true, inv);
             for (int q = 0; q < 6; ++q) t.L[(size_t)q * k.n + i] = inv[q];
@@ -1945,22 +1948,27 @@ bool fp32_rebuild_due(Fp32State& st, cudaStream_t s) {
 // Grids of the main passes cover the largest possible count of listed static particles;
 // the threads past the device count return at once.
 // skip_fluid: the first rates pass computes the fluid's factors; when the dynamic block holds
-// fluid only, the main pass then visits the listed static particles alone.
+// fluid only, the main pass then visits the listed static particles alone.  skip_static:
+// the first boundary pass computes the static block's Shepard factors.
 template <int DIM>
-void corr_launch(Fp32State& st, cudaStream_t s, const Ovf& ovf, bool skip_fluid) {
+void corr_launch(Fp32State& st, cudaStream_t s, const Ovf& ovf, bool skip_fluid, bool skip_static) {
     const K32& k = st.k;
     const P32& p = st.P[st.cur];
     const int lim = skip_fluid && st.c.n_bdy <= k.n - k.nd ? 0 : k.nd;
-    const int nb = nblk(lim + (k.n - k.nd), st.tpb);
+    const int* act = skip_static ? nullptr : st.sact;
+    const int nmax = skip_static ? k.nd : k.n;
+    const int nb = nblk(lim + (skip_static ? 0 : k.n - k.nd), st.tpb);
     const int sf = skip_fluid ? 1 : 0;
-    if (k.kernel == 1)
-        TSG_LAUNCH((k_corr32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact,
-                   lim, sf, ovf);
-    else
-        TSG_LAUNCH((k_corr32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact,
-                   lim, sf, ovf);
-    TSG_LAUNCH((k_corr32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.sact, st.nsact, lim, sf,
-               ovf);
+    if (nb > 0) {
+        if (k.kernel == 1)
+            TSG_LAUNCH((k_corr32<DIM, false, 1>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, act, st.nsact,
+                       lim, nmax, sf, ovf);
+        else
+            TSG_LAUNCH((k_corr32<DIM, false, 0>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, act, st.nsact,
+                       lim, nmax, sf, ovf);
+    }
+    TSG_LAUNCH((k_corr32<DIM, true, -1>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, act, st.nsact, lim, nmax,
+               sf, ovf);
 }
 
 // WCSPH boundary extrapolation over [base, base + count_n); the static block (base = nd)
@@ -1998,15 +2006,15 @@ void rates_launch(Fp32State& st, const P32& p, cudaStream_t s, const Ovf& ovf) {
     TSG_LAUNCH((k_rates32<DIM, true, CORR, -1, -1, FL>), 64, TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf);
 }
 
-static void kernel_corr(Fp32State& st, cudaStream_t s, bool skip_fluid) {
+static void kernel_corr(Fp32State& st, cudaStream_t s, bool skip_fluid, bool skip_static) {
     PhaseScope ph(s, PH_CORR);
     const K32& k = st.k;
     const Ovf ovf{st.ovf_list, st.novf};
-    if (k.dim == 2) corr_launch<2>(st, s, ovf, skip_fluid);
-    else corr_launch<3>(st, s, ovf, skip_fluid);
+    if (k.dim == 2) corr_launch<2>(st, s, ovf, skip_fluid, skip_static);
+    else corr_launch<3>(st, s, ovf, skip_fluid, skip_static);
 }
 
-void fp32_kernel_corr(Fp32State& st, cudaStream_t s) { kernel_corr(st, s, false); }
+void fp32_kernel_corr(Fp32State& st, cudaStream_t s) { kernel_corr(st, s, false, false); }
 
 void fp32_init_tmp(Fp32State& st, cudaStream_t s) {
     PhaseScope ph(s, PH_INIT);
@@ -2090,8 +2098,8 @@ static void one_step(Fp32State& st, cudaStream_t s, bool eos, bool fl = false, b
         PhaseScope ph(s, PH_RATES);
         const Ovf ovf{st.ovf_list, st.novf};
         if (fl) {
-            if (k.dim == 2) rates_launch<2, true, true>(st, p, s, ovf);
-            else rates_launch<3, true, true>(st, p, s, ovf);
+            if (k.dim == 2) { if (k.corr) rates_launch<2, true, true>(st, p, s, ovf); else rates_launch<2, false, true>(st, p, s, ovf); }
+            else { if (k.corr) rates_launch<3, true, true>(st, p, s, ovf); else rates_launch<3, false, true>(st, p, s, ovf); }
         } else if (k.dim == 2) { if (k.corr) rates_launch<2, true>(st, p, s, ovf); else rates_launch<2, false>(st, p, s, ovf); }
         else { if (k.corr) rates_launch<3, true>(st, p, s, ovf); else rates_launch<3, false>(st, p, s, ovf); }
     }
@@ -2158,13 +2166,15 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
     // WCSPH with symplectic Euler or leap-frog: the fluid EOS (first phase of each one_step)
     // runs inside init_real2tmp and the half step, which produce its input density_tmp
     const bool fuse = st.k.solver == 1 && st.c.ti != 4;
-    // WCSPH leap-frog with CSPM: the fluid's CSPM factors come from the first rates pass
-    // (positions stay fixed through both one_steps, so the second pass reads them back)
-    const bool fuse_corr = fuse && st.c.ti == 2 && st.k.corr == 1;
-    // ... and when the dynamic block holds fluid only, the static block's Shepard factors
-    // come from the first boundary pass, which leaves the correction kernel nothing to do
-    const bool fuse_shep = fuse_corr && st.c.n_bdy <= st.k.n - st.k.nd;
-    if (!fuse_shep) kernel_corr(st, s, fuse_corr);
+    // The fluid's CSPM factors come from the first rates pass (positions stay fixed through
+    // the step, so a second pass reads them back), except with symplectic Euler and CSPM,
+    // whose single pass updates the density from the continuity sum and so keeps the
+    // compensated per-neighbour form; and when the dynamic block holds fluid only, the
+    // static block's Shepard factors come from the first boundary pass.  With both, the
+    // correction kernel has nothing left to do.
+    const bool fuse_corr = fuse && (st.c.ti == 2 || st.k.corr == 0);
+    const bool fuse_shep = fuse && st.c.n_bdy <= st.k.n - st.k.nd;
+    if (!(fuse_corr && fuse_shep)) kernel_corr(st, s, fuse_corr, fuse_shep);
     if (fuse) {
         PhaseScope ph(s, PH_INIT);
         TSG_LAUNCH(k_init_tmp32<true>, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T);
