@@ -23,6 +23,8 @@
   the dynamic block holding fluid only, the dummies' Shepard factors come from the first
   boundary pass; with a static rigid obstacle in the dynamic block the correction kernel
   still runs for the non-fluid particles.  The obstacle scene also against the f64 oracle.
+  A doubly dense block, whose fluid lists overflow, takes the same checks through the
+  kernels' overflow passes (2 steps, and against the oracle).
 * Threads per block changes no arithmetic: bit-identical.  Cells per CTA of the list
   build (and the per-particle builder) give the same neighbour sets; the entries of a list
   may be ordered differently, so steps agree within 1e-6 relative.
@@ -223,6 +225,52 @@ def test_fused_cspm_step_matches_stage_calls(native, case):
         pa, pb = a.ps.field("pressure").cpu().numpy()[f], b.ps.field("pressure").cpu().numpy()[f]
         np.testing.assert_allclose(pa, pb, rtol=1e-7, atol=1e-4)
         np.testing.assert_allclose(a.ps.field("x").cpu().numpy(), b.ps.field("x").cpu().numpy(), rtol=0, atol=1e-9)
+
+
+def _dense(d):
+    """A second fluid block over the first, offset by half a spacing in x and y: every fluid
+    particle has about twice the lattice's neighbours, more than a list holds, so the list
+    kernels serve them from their overflow passes (direct cell traversal).  Densities start
+    at the rest density (they evolve by continuity), so the block starts at rest."""
+    import copy
+    h = d["Configuration"]["particleRadius"]
+    b = copy.deepcopy(d["Blocks"][0])
+    b["translation"] = [b["translation"][0] + h, b["translation"][1] + h, b["translation"][2]]
+    d["Blocks"].append(b)
+    return d
+
+
+def test_fused_cspm_overflow_passes(oracle_lib, native):
+    d = _dense(small_dambreak_2d(corr=1))
+    d["Configuration"]["neighbourSkin"] = 0.0
+    a, b = _single(d), _single(d)
+    a.ps.initialize_particle_system()
+    assert a.ps.list_stats()["overflowed"] > 100
+    for step in range(2):
+        a.solver.step(1)
+        _stage_step(b)
+        np.testing.assert_array_equal(a.ps.field("id0").cpu().numpy(), b.ps.field("id0").cpu().numpy())
+        if step == 0:
+            for nm in ("CSPM_f", "CSPM_L"):
+                np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy(),
+                                              err_msg=nm)
+        f = a.ps.field("mat_type").cpu().numpy() == 1
+        ra, rb = a.ps.field("density_tmp").cpu().numpy()[f], b.ps.field("density_tmp").cpu().numpy()[f]
+        assert np.max(np.abs(ra - rb) / rb) < 1e-9, (step, np.max(np.abs(ra - rb) / rb))
+        pa, pb = a.ps.field("pressure").cpu().numpy()[f], b.ps.field("pressure").cpu().numpy()[f]
+        np.testing.assert_allclose(pa, pb, rtol=1e-6, atol=1e-3)
+    a.ps.check_errors()
+    orc = oracle_lib.OracleSim(cfg_of(d))
+    orc.step(2)
+    ids = orc.get("id0").astype(np.int64)
+    def by_id(v):
+        out = np.empty_like(v)
+        out[ids] = v
+        return out
+    f = by_id(orc.get("mat_type")) == 1
+    rho_o, x_o = by_id(orc.get("density")), by_id(orc.get("x"))
+    assert np.max(np.abs(_by_id0(a.ps, "density")[f] - rho_o[f]) / rho_o[f]) < 1e-5
+    assert np.max(np.abs(_by_id0(a.ps, "x")[f] - x_o[f])) < 1e-6
 
 
 def test_fused_cspm_obstacle_vs_oracle(oracle_lib, native):
