@@ -529,12 +529,12 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         const float rti = k.rho0 + t.drt[i];
         const float visc_b = k.rho0 / rti;
         float L[9];
-        if (CORR && !FL)
+        if (CORR && !FLC)
             load_L(t.L, k.n, i, L);
         CSum dd, dv[3];
         CSum sh;                                 // FL: Shepard sum
-        float A[6] = {0, 0, 0, 0, 0, 0};         // FL: continuity tensor (symmetric part)
-        float M[6] = {0, 0, 0, 0, 0, 0};         // FL: CSPM matrix
+        float A[6] = {0, 0, 0, 0, 0, 0};         // FLC: continuity tensor (symmetric part)
+        float M[6] = {0, 0, 0, 0, 0, 0};         // FLC: CSPM matrix
         const bool rep_on = REP < 0 ? (k.boundary == 3 || k.boundary == 4) : REP == 1;
         // viscosity factor for fluid and for boundary neighbours; -rho0 p_i / rho_i^2
         const float vf_f = visc_fac, vf_b = visc_fac * visc_b;
@@ -547,8 +547,8 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
             const float mg = __fmul_rn(wg.g, mVj);   // m_Vj G, grad W = G d
             const float dvx = vti.x - vtj.x, dvy = vti.y - vtj.y, dvz = DIM == 3 ? vti.z - vtj.z : 0.f;
             const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
-            // WCSPH scenes hold no soil: the flow neighbours are the fluid ones
             const float e[3] = {__fmul_rn(mg, d[0]), __fmul_rn(mg, d[1]), __fmul_rn(mg, d[2])};
+            // WCSPH scenes hold no soil: the flow neighbours are the fluid ones
             if (FL) cspm_terms<DIM>(sh, M, d, e, wg.w, mVj, cj == kCodeFluid, CORR && cj == kCodeFluid);
             if (FLC) {
                 const float dvv[3] = {dvx, dvy, dvz};
