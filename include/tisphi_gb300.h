@@ -157,7 +157,11 @@ int tsg_advect(tsg_handle* h, int which, void* stream);
  * (eng/solver_sph_base.py:53-61, :89-91, :116-120, :172-180). */
 int tsg_substep(tsg_handle* h, void* stream);
 
-/* nsteps x SPHBase.step (eng/solver_sph_base.py:41-51). */
+/* nsteps x SPHBase.step (eng/solver_sph_base.py:41-51).  The FP32-mixed WCSPH step
+ * (symplectic Euler or leap-frog) computes the Shepard factors, and with leap-frog the
+ * CSPM matrices, inside its first rates and boundary passes instead of a separate
+ * correction pass; the factors equal tsg_kernel_corr's bit for bit, and the fields hold
+ * them after the step as in the reference. */
 int tsg_step(tsg_handle* h, int nsteps, void* stream);
 
 /* Device view of a named particle field in the current (cell-sorted) order.  Replaces
