@@ -459,8 +459,8 @@ __global__ void k_pre32(K32 k, P32 p, T32 t) {
 // Boundary extrapolation for dummy / repulsive / rigid particles in [base, base + count_n) (WC).
 // SH: the particle's Shepard factor is summed in the same loop (its list holds flow
 // neighbours only, in the correction kernel's order, so the factor has the same bits) and
-// stored, instead of read (the first one_step of a leap-frog WCSPH step with CSPM, whose
-// correction kernel then has nothing left to visit in the static block).
+// stored, instead of read (the first one_step of a WCSPH step, whose correction kernel
+// then skips the static block).
 template <int DIM, bool FB, int KT, bool SH = false>
 __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                         const int* __restrict__ sstart, int base, int count_n, const int* __restrict__ act,
