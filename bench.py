@@ -178,7 +178,7 @@ def cpu_baseline(cfg_dict, budget_s=25.0):
 
 
 # ---------------------------------------------------------------- GPU measurement
-def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None, fused_corr=False):
+def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None, fused=None):
     """Unique bytes a kernel must move once per launch (neighbour re-reads excluded).
 
     Every per-particle array the kernel touches counts once (read or written), as does
@@ -199,10 +199,14 @@ def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None, fuse
               CSPM_f (4) and the writes (v_tmp, p / rho^2) (16), (p, rho) (8),
               density_tmp (4), pressure (4); per flow particle lo + v_tmp + (p, rho)
               (16 + 16 + 8); plus the dummies' list entries.
-    fused_corr (FP32-mixed leap-frog with CSPM: the first rates pass computes the flow
-    particles' CSPM factors): the rates figure is the mean of the two passes, the first
-    writing CSPM_f (4) and CSPM_L (24) instead of reading CSPM_L (24), so 26 B per flow
-    particle; the correction kernel visits the listed dummies only.
+    fused ("se" / "lf": the FP32-mixed WCSPH step, whose first rates pass computes the flow
+    particles' Shepard factors, and with leap-frog + CSPM their CSPM matrices, and whose
+    first boundary pass the dummies' Shepard factors): the rates figure is the mean over the
+    step's rates passes — leap-frog: the first writes CSPM_f (4) and, with CSPM, CSPM_L (24)
+    where the second reads CSPM_L (24), so 2 + 24 B per flow particle; symplectic Euler:
+    the one pass writes CSPM_f (4) and reads CSPM_L (24 with CSPM).  The boundary pass
+    writes the Shepard factor where it would read it (same bytes).  The correction kernel
+    runs only with symplectic Euler + CSPM, over the flow particles.
     """
     if precision == "fp64":
         if kernel != "rates":
@@ -213,11 +217,16 @@ def algorithmic_bytes(kernel, n_total, n_flow, precision, corr, lists=None, fuse
     na = lists.get("listed_dummies", n_total - n_flow)
     n_vis = n_flow + na
     if kernel == "rates":
-        cspm = (26 if fused_corr else 24) if corr else 0
+        if fused == "lf":
+            cspm = 2 + (24 if corr else 0)
+        elif fused == "se":
+            cspm = 4 + (24 if corr else 0)
+        else:
+            cspm = 24 if corr else 0
         return n_vis * 32 + n_flow * (16 + 4 + 4 + cspm + 20) + 4 * er
     if kernel == "kernel_corr":
-        if fused_corr:
-            return na * (36 + 4 + 24 + 4) + 4 * ed
+        if fused:
+            return n_flow * (36 + 4 + (24 if corr else 0)) + 4 * er
         return n_vis * (36 + 4 + (24 if corr else 0)) + na * 4 + 4 * (er + ed)
     if kernel == "boundary":
         return na * (4 + 48 + 4 + 4 + 32) + n_flow * 40 + 4 * ed
@@ -423,8 +432,11 @@ def run_ours(args):
     n_flow = h["n_fluid"]
     def roof(kernel):
         ph = h["phases"].get(kernel)
-        fused = head == "fp32_mixed" and corr and cfg_dict["Configuration"].get("timeIntegration") == 2 \
-            and cfg_dict["Configuration"].get("simulationMethod", 1) == 1
+        conf = cfg_dict["Configuration"]
+        ti = conf.get("timeIntegration")
+        fused = None
+        if head == "fp32_mixed" and conf.get("simulationMethod", 1) == 1 and ti in (1, 2):
+            fused = "lf" if ti == 2 else "se"
         alg = algorithmic_bytes(kernel, h["n_total"], n_flow, head, corr, h.get("lists"), fused)
         if not ph or not alg or not ph["ms_per_launch"]:
             return None
