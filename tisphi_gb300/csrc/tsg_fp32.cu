@@ -1013,16 +1013,33 @@ __global__ void k_advect_full32(K32 k, P32 p, T32 t, int* err) {
     if (!isfinite(dr)) atomicOr(err, TSG_ERR_NONFINITE);
 }
 
-// WCSPH without XSPH, symplectic Euler or leap-frog: advect_SE / advect_LF, advect_pos and
-// the density clamp of advect_something in one pass over each particle's own state, in
-// the order of the separate kernels.  The velocity and position updates are explicit fused
-// multiply-adds here and there, so the compiler's contraction choices cannot make the two
-// paths round differently.
-__global__ void k_advect_final_wc32(K32 k, P32 p, T32 t, int* err) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.nd) return;
-    const int ti = tf_type(p.hi[i].w);
-    if (ti <= 0) return;
+// Largest squared displacement of a real particle since the last list build (pf holds the
+// build-time positions); float bits of non-negative values order like unsigned integers.
+// block_max_disp is called by every thread of the block (one atomic per block: a warp's
+// atomics on the one word serialise); the rounding of disp2 is spelled out so that the
+// kernels computing it give the same bits.
+__device__ __forceinline__ float disp2(const float4& h, const float4& l, const float4& f) {
+    const float dx = __fsub_rn(__fadd_rn(h.x, l.x), f.x), dy = __fsub_rn(__fadd_rn(h.y, l.y), f.y),
+                dz = __fsub_rn(__fadd_rn(h.z, l.z), f.z);
+    const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    return d2 == d2 ? d2 : 3.0e38f;  // non-finite: force a rebuild (the hash flags it)
+}
+__device__ __forceinline__ void block_max_disp(float d2, unsigned* maxd) {
+    __shared__ float wmax[32];
+    for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0) wmax[w] = d2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = 0.f;
+        for (int q = 0; q < nw; ++q) m = fmaxf(m, wmax[q]);
+        if (m > 0.f) atomicMax(maxd, __float_as_uint(m));
+    }
+}
+
+// One real particle's advect_SE / advect_LF, advect_pos and density clamp; returns the new
+// (lo, m_V) record.
+__device__ __forceinline__ float4 advect_final_one(const K32& k, P32& p, T32& t, int i, int ti, int* err) {
     float dr = p.drho[i] + k.dt * t.dd[i];
     const bool dr_ok = isfinite(dr);
     const float4 dv = t.dv[i];
@@ -1049,6 +1066,29 @@ __global__ void k_advect_final_wc32(K32 k, P32 p, T32 t, int* err) {
     l.w = p.mass[i] / (k.rho0 + dr);
     p.lo[i] = l;
     if (!dr_ok || !(isfinite(l.x) && isfinite(l.y) && isfinite(l.z))) atomicOr(err, TSG_ERR_NONFINITE);
+    return l;
+}
+
+// WCSPH without XSPH, symplectic Euler or leap-frog: advect_SE / advect_LF, advect_pos and
+// the density clamp of advect_something in one pass over each particle's own state, in
+// the order of the separate kernels.  The velocity and position updates are explicit fused
+// multiply-adds here and there, so the compiler's contraction choices cannot make the two
+// paths round differently.  maxd (may be null): the largest squared displacement since the
+// list build is folded in from the new positions, as the next step's list-expiry check
+// would compute it (a captured multi-step graph drops that check after its first step
+// and has the steps before the last fold their positions in).
+__global__ void k_advect_final_wc32(K32 k, P32 p, T32 t, int* err, const float4* __restrict__ PF,
+                                    unsigned* __restrict__ maxd) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.f;
+    if (i < k.nd) {
+        const float4 h = p.hi[i];
+        if (tf_type(h.w) > 0) {
+            const float4 l = advect_final_one(k, p, t, i, tf_type(h.w), err);
+            if (maxd) d2 = disp2(h, l, PF[i]);
+        }
+    }
+    if (maxd) block_max_disp(d2, maxd);
 }
 
 template <int DIM, bool FB>
@@ -1409,20 +1449,13 @@ __global__ void k_nbr_fill_ell(K32 k, const float4* HI, const float4* LO, const 
     }
 }
 
-// Largest squared displacement of a real particle since the last list build (pf holds the
-// build-time positions); float bits of non-negative values order like unsigned integers.
+// Largest squared displacement of a real particle since the last list build.
 __global__ void k_disp32(K32 k, const float4* __restrict__ HI, const float4* __restrict__ LO,
                          const float4* __restrict__ PF, unsigned* __restrict__ maxd) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     float d2 = 0.f;
-    if (i < k.nd) {
-        const float4 h = HI[i], l = LO[i], f = PF[i];
-        const float dx = (h.x + l.x) - f.x, dy = (h.y + l.y) - f.y, dz = (h.z + l.z) - f.z;
-        d2 = dx * dx + dy * dy + dz * dz;
-        if (!(d2 == d2)) d2 = 3.0e38f;  // non-finite: force a rebuild (the hash flags it)
-    }
-    for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
-    if ((threadIdx.x & 31) == 0 && d2 > 0.f) atomicMax(maxd, __float_as_uint(d2));
+    if (i < k.nd) d2 = disp2(HI[i], LO[i], PF[i]);
+    block_max_disp(d2, maxd);
 }
 
 // List occupancy: out[0] / out[1] += stored entries (min(count, capacity)) of the dynamic /
@@ -2162,7 +2195,9 @@ void fp32_rk_update(Fp32State& st, int m, cudaStream_t s) {
 // One SPHBase.step() after the (conditional) re-sort: kernel correction, init_real2tmp,
 // the integrator's one_step / advect sequence, advect_pos, advect_something and, in
 // collision mode, enforce_boundary (eng/solver_sph_base.py:41-61, :79-120).
-void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
+// fold_disp: the fused final update folds the new positions into the displacement maximum
+// (the next step, captured in the same graph, skips its list-expiry check).
+void f32::step_body(Fp32State& st, cudaStream_t s, bool collide, bool fold_disp) {
     // WCSPH with symplectic Euler or leap-frog: the fluid EOS (first phase of each one_step)
     // runs inside init_real2tmp and the half step, which produce its input density_tmp
     const bool fuse = st.k.solver == 1 && st.c.ti != 4;
@@ -2203,7 +2238,8 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide) {
         }
         if (fuse && !st.k.xsph) {  // advect_SE / _LF, advect_pos and the WCSPH clamp at once
             PhaseScope ph(s, PH_INTEGRATE);
-            TSG_LAUNCH(k_advect_final_wc32, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T, st.err);
+            TSG_LAUNCH(k_advect_final_wc32, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T, st.err, st.pf,
+                       fold_disp ? st.maxdisp : nullptr);
             if (st.k.disp2_limit <= 0.f) st.lists_valid = false;
             if (collide) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
             return;
@@ -2237,6 +2273,12 @@ void fold_rebuilds(Fp32State& st, cudaStream_t s) {
 }
 
 // Capture `steps` steps into one executable graph.  Each step: displacement check, then an
+// Whether step_body ends with the fused final update (which folds the new positions into
+// the displacement maximum) and moves no particle after it.
+bool folds_disp(const Fp32State& st, bool collide) {
+    return st.k.solver == 1 && st.c.ti != 4 && !st.k.xsph && !collide && st.k.disp2_limit > 0.f;
+}
+
 // IF node whose body re-sorts in place and rebuilds the lists, then the step body.
 int capture_steps(Fp32State& st, int steps, bool collide, Fp32State::StepGraph& g) {
     cudaStream_t cs = nullptr, bs = nullptr;
@@ -2255,7 +2297,10 @@ int capture_steps(Fp32State& st, int steps, bool collide, Fp32State::StepGraph& 
         cudaGraphConditionalHandle hnd;
         if (cudaGraphConditionalHandleCreate(&hnd, cg, 0, cudaGraphCondAssignDefault) != cudaSuccess) { rc = TSG_E_CUDA; break; }
         P32& p = st.P[st.cur];
-        TSG_LAUNCH(k_disp32, nblk(k.nd), TPB, cs, k, p.hi, p.lo, st.pf, st.maxdisp);
+        // after the first step of the graph, the previous step's fused final update has folded
+        // its new positions into the displacement maximum already
+        if (q == 0 || !folds_disp(st, collide))
+            TSG_LAUNCH(k_disp32, nblk(k.nd), TPB, cs, k, p.hi, p.lo, st.pf, st.maxdisp);
         TSG_LAUNCH(k_set_rebuild32, 1, 1, cs, hnd, st.maxdisp, k.disp2_limit, st.d_rebuilds);
         const cudaGraphNode_t* deps = nullptr;
         size_t ndeps = 0;
@@ -2284,7 +2329,7 @@ int capture_steps(Fp32State& st, int steps, bool collide, Fp32State::StepGraph& 
         cudaGraph_t done = nullptr;
         if (cudaStreamEndCapture(bs, &done) != cudaSuccess) { rc = TSG_E_CUDA; break; }
         body = launch_total() - b0;
-        step_body(st, cs, collide);
+        step_body(st, cs, collide, q + 1 < steps && folds_disp(st, collide));
     }
     cudaError_t e = cudaStreamEndCapture(cs, &graph);
     if (!rc && (e != cudaSuccess || !graph)) rc = TSG_E_CUDA;

@@ -565,7 +565,7 @@ namespace f32 {
 // Re-sort the dynamic block and rebuild every list (in_place keeps the current buffer).
 void rebuild(Fp32State& st, cudaStream_t s, bool in_place);
 // One step after the re-sort: correction, init_real2tmp, integrator, advect_pos, post-step.
-void step_body(Fp32State& st, cudaStream_t s, bool collide);
+void step_body(Fp32State& st, cudaStream_t s, bool collide, bool fold_disp = false);
 }  // namespace f32
 
 }  // namespace tsg
