@@ -153,6 +153,11 @@ int tsg_one_step(tsg_handle* h, void* stream);
 /* Per-particle update selected by TSG_ADVECT_*; see the enum for the reference kernels. */
 int tsg_advect(tsg_handle* h, int which, void* stream);
 
+/* d_density_RK += m d_density, d_vel_RK += m d_vel, d_stress_RK += m d_stress for real
+ * particles, m = 1 or 2.  Replaces update_RK (eng/solver_sph_base.py:153-160); with the
+ * TSG_RK_* advect calls it lets a caller run substep_RK on a handle of any integrator. */
+int tsg_rk_update(tsg_handle* h, int32_t m, void* stream);
+
 /* substep(): SE / LF / RK4 sequence of one_step and advect calls
  * (eng/solver_sph_base.py:53-61, :89-91, :116-120, :172-180). */
 int tsg_substep(tsg_handle* h, void* stream);
@@ -184,6 +189,16 @@ int tsg_grid(tsg_handle* h, int32_t* out, void* stream);
  * Host copies; synchronises.  *total receives the number of pairs; list may be NULL to
  * query it; returns TSG_E_CAPACITY when cap is too small. */
 int tsg_neighbors(tsg_handle* h, int32_t* counts, int32_t* list, int64_t cap, int64_t* total, void* stream);
+
+/* Density summation: out[i] = sum over the neighbours j != i of particle i (support radius,
+ * the reference's traversal) of mass_j W(x_i - x_j), for every particle, in the current
+ * particle order (the order of tsg_field views).  out is a device array of n doubles.
+ * Replaces WCSPHSolver.calc_density_task summed by for_all_neighbors
+ * (eng/solver_sph_wc.py:30-31, eng/particle_system.py:259-269), which the reference
+ * defines but never calls from a step; like it, the sum has no self term and dummy
+ * particles carry zero mass.  FP64 form: bit-identical to the f64 reference order; FP32-mixed
+ * form: compensated f32 sums.  Needs a sorted state (tsg_sort or a step). */
+int tsg_density_sum(tsg_handle* h, double* out, void* stream);
 
 /* FP64 diagnostics over flow particles: out[0] total mass, out[1..3] momentum,
  * out[4] kinetic energy, out[5] potential energy (-m g.x), out[6] max |v|,
@@ -248,8 +263,11 @@ int tsg_profile_read(double* ms, int64_t* counts, int nphase);
  * per GPU, held until the process exits), so n must not exceed TSG_NOALLOC_MAX_PARTICLES
  * and grid_num_total + 1 must not exceed TSG_NOALLOC_MAX_CELLS (else TSG_E_CAPACITY).
  * Every call shares that scratch, so calls that overlap on the GPU race.  The first call
- * on a device looks up the scratch address (once per device); make it before any stream
- * capture begins. */
+ * on a device looks up the scratch address (once per device, kept for the life of the
+ * process, so do not call it again after a cudaDeviceReset); make it before any stream
+ * capture begins.  Unlike tsg_sort it raises no status for particles outside the grid or
+ * with non-finite positions: they land in the trailing bin in ascending index order, and
+ * cell_start[grid_num_total + 1] - cell_start[grid_num_total] counts them. */
 #define TSG_NOALLOC_MAX_PARTICLES 262144
 #define TSG_NOALLOC_MAX_CELLS 262144
 int tsg_sort_noalloc(const tsg_config* cfg, const double* x, int64_t n, int32_t* cell_start, int32_t* perm,

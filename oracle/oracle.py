@@ -70,6 +70,7 @@ def lib():
         L.orc_neighbors.restype = ctypes.c_long
         L.orc_neighbors.argtypes = [P, ip, ip, ctypes.c_long]
         L.orc_error.argtypes = [P]
+        L.orc_density_sum.argtypes = [P, ctypes.POINTER(ctypes.c_double)]
         _lib = L
     return _lib
 
@@ -188,6 +189,12 @@ class OracleSim:
         lst = np.zeros(max(total, 1), dtype=np.int32)
         lib().orc_neighbors(self.h, counts.ctypes.data_as(ip), lst.ctypes.data_as(ip), total)
         return counts, lst[:total]
+
+    def density_sum(self):
+        """calc_density_task summed over every particle's neighbours (current order)."""
+        out = np.zeros(self.n, dtype=np.float64)
+        lib().orc_density_sum(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return out
 
     def error(self):
         return lib().orc_error(self.h)

@@ -959,6 +959,20 @@ long orc_neighbors(void* h, int* counts, int* list, long cap) {
     return (list && total > cap) ? -1 : total;
 }
 
+// Density summation: calc_density_task summed by for_all_neighbors
+// (eng/solver_sph_wc.py:30-31, eng/particle_system.py:259-269), ret += mass_j W(x_i - x_j)
+// in traversal order, for every particle.
+int orc_density_sum(void* h, double* out) {
+    Sys* s = static_cast<Sys*>(h);
+#pragma omp parallel for
+    for (int i = 0; i < s->n; ++i) {
+        double ret = 0.0;
+        s->for_all_neighbors(i, [&](int j) { ret += s->pt[j].mass * s->W(vsub(s->pt[i].x, s->pt[j].x)); });
+        out[i] = ret;
+    }
+    return 0;
+}
+
 int orc_error(void* h) { return static_cast<Sys*>(h)->err; }
 
 }  // extern "C"

@@ -56,6 +56,7 @@ int orc_steps(void* h, int nsteps);
 int orc_get(void* h, const char* name, double* out);
 int orc_grid(void* h, int* out);
 long orc_neighbors(void* h, int* counts, int* list, long cap);
+int orc_density_sum(void* h, double* out);
 int orc_error(void* h);
 
 #ifdef __cplusplus

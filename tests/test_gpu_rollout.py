@@ -132,3 +132,29 @@ def test_column_2000_steps_fp32_mixed_vs_fp64(native, method):
     report = f"method {method}: drift {dr}, mean strain_equ {eq}, errors {err}"
     assert abs(dr["fp32_mixed"]["front"] - dr["fp64"]["front"]) <= 0.1 * 0.002, report
     assert abs(eq["fp32_mixed"] - eq["fp64"]) <= 1e-2 * abs(eq["fp64"]), report
+
+
+def test_column_stated_size_mui_fp32_mixed_vs_fp64(native):
+    """The granular column of the benchmark configuration at its stated size: mu(I), spacing
+    0.001 m (20,000 soil particles), symplectic Euler at dt 1e-5, here over the first 1,000
+    of its 6,100 steps (the full run is bench.py --workload column): runout within 0.1
+    spacing and mean equivalent strain within 1 % of the FP64 form."""
+    import torch
+
+    from tisphi_gb300 import compare, scenes
+    from tisphi_gb300.simulation import Simulation
+    cfg = cfg_of(scenes.column_2d(method=2, spacing=0.001, dt=1e-5, integration=1))
+    sims = {p: Simulation(cfg, precision=p) for p in ("fp32_mixed", "fp64")}
+    assert int(np.count_nonzero(sims["fp64"].ps.scene.mat_type == 2)) == 20000
+    d0 = {p: s.ps.diagnostics() for p, s in sims.items()}
+    for s in sims.values():
+        s.solver.step(1000)
+    torch.cuda.synchronize()
+    dr = {p: compare.drift(d0[p], s.ps.diagnostics()) for p, s in sims.items()}
+    eq = {}
+    for p, s in sims.items():
+        mt = s.ps.field("mat_type").cpu().numpy()
+        eq[p] = float(s.ps.field("strain_equ").cpu().numpy()[mt == 2].mean())
+    report = f"drift {dr}, mean strain_equ {eq}"
+    assert abs(dr["fp32_mixed"]["front"] - dr["fp64"]["front"]) <= 0.1 * 0.001, report
+    assert eq["fp64"] > 0 and abs(eq["fp32_mixed"] - eq["fp64"]) <= 1e-2 * eq["fp64"], report

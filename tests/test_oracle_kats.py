@@ -230,3 +230,42 @@ def test_hydrostatic_column(oracle_lib):
     depth = y[fluid].max() - y[fluid]
     slope = np.polyfit(depth, p_mean[fluid], 1)[0]
     assert abs(slope / (1000.0 * 9.81) - 1.0) < 0.1, f"dp/ddepth = {slope:.1f} Pa/m"
+
+
+@pytest.mark.parametrize("dim,kernel", [(2, 1), (2, 0), (3, 1)])
+def test_density_sum_matches_brute_force(oracle_lib, dim, kernel):
+    """The oracle's density summation (calc_density_task over for_all_neighbors,
+    eng/solver_sph_wc.py:30-31) equals an independent numpy sum over all pairs j != i
+    closer than the support radius of mass_j W(|x_i - x_j|), on a jittered scene; and on
+    the unjittered lattice an interior 2D fluid particle sums to rho0 (1 - dx^2 W(0)): the
+    sum has no self term."""
+    if dim == 2:
+        d = scenes.dambreak_2d(spacing=0.02, width=0.3, height=0.2, domain=(0.6, 0.4), kernel=kernel)
+    else:
+        d = scenes.dambreak_3d(spacing=0.02, domain=(0.3, 0.2, 0.2), size=(0.12, 0.1, 0.08))
+    cfg = cfg_of(d)
+    orc = oracle_lib.OracleSim(cfg)
+    orc.sort()
+    got = orc.density_sum()
+    x, mass = orc.get("x"), orc.get("mass")
+    from tisphi_gb300.scene import scene_geometry
+    geo = scene_geometry(cfg)
+    h, R = geo.smoothing_len, geo.support_radius
+    diff = x[:, None, :] - x[None, :, :]
+    r = np.sqrt(np.einsum("ijk,ijk->ij", diff, diff))
+    np.fill_diagonal(r, np.inf)
+    w, _ = _kernel(dim, kernel, h, np.where(r < R, r, 0.0))
+    want = np.where(r < R, w * mass[None, :], 0.0).sum(axis=1)
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-9)
+    if dim == 2 and kernel == 1:
+        lat = cfg_of(scenes.dambreak_2d(spacing=0.02, width=0.6, height=0.4, domain=(1.2, 0.8), jitter=0.0))
+        o2 = oracle_lib.OracleSim(lat)
+        o2.sort()
+        rho = o2.density_sum()
+        full, _ = _lattice_moments(2, 1, 0.02, h, R)
+        w0, _ = _kernel(2, 1, h, np.zeros(1))
+        expect = 1000.0 * (full - 0.02 ** 2 * w0[0])
+        xs, mt = o2.get("x"), o2.get("mat_type")
+        mid = (mt == 1) & (np.abs(xs[:, 0] - 0.3) < 0.05) & (np.abs(xs[:, 1] - 0.2) < 0.05)
+        assert mid.any()
+        np.testing.assert_allclose(rho[mid], expect, rtol=1e-9)

@@ -119,10 +119,9 @@ int alloc_all(tsg_handle* h) {
     rc |= dalloc(h, &t.CSPM_f, n);
     if (c.corr == 1) rc |= dalloc(h, &t.CSPM_L, 9 * n);
     rc |= dalloc(h, &t.d_strain_equ, n); rc |= dalloc(h, &t.d_strain_equ_p, n);
-    if (c.ti == 4) {
-        rc |= dalloc(h, &t.d_density_RK, n); rc |= dalloc(h, &t.d_vel_RK, 3 * n);
-        if (c.solver == 3) rc |= dalloc(h, &t.d_stress_RK, 9 * n);
-    }
+    // RK4 accumulators for every integrator: substep_RK may be called on any handle
+    rc |= dalloc(h, &t.d_density_RK, n); rc |= dalloc(h, &t.d_vel_RK, 3 * n);
+    if (c.solver == 3) rc |= dalloc(h, &t.d_stress_RK, 9 * n);
     rc |= dalloc(h, &t.aux3, 3 * n);
     rc |= dalloc(h, &t.pos32, n);
     Grid& g = h->g;
@@ -396,7 +395,6 @@ int tsg_advect(tsg_handle* h, int which, void* stream) {
     if (!h || !h->uploaded) return TSG_E_STATE;
     if (which < TSG_ADVECT_FULL || which > TSG_RK_FINAL) return TSG_E_ARG;
     if ((which == TSG_ADVECT_POS || which == TSG_ADVECT_SOMETHING) && !h->sorted) return TSG_E_STATE;
-    if (which >= TSG_RK_INIT && h->c.ti != 4) return TSG_E_STATE;  // RK buffers exist only for RK4
     cudaStream_t s = S(stream);
     if (use_fp32(h)) {
         fp32_advect(*h->f32, which, s);
@@ -411,6 +409,13 @@ int tsg_advect(tsg_handle* h, int which, void* stream) {
 static void rk_update(tsg_handle* h, int m, cudaStream_t s) {
     if (use_fp32(h)) fp32_rk_update(*h->f32, m, s);
     else fp64_rk_update(h->c, h->cur, h->t, m, s);
+}
+
+int tsg_rk_update(tsg_handle* h, int32_t m, void* stream) {
+    if (!h || !h->uploaded) return TSG_E_STATE;
+    if (m < 1 || m > 2) return TSG_E_ARG;
+    rk_update(h, m, S(stream));
+    return check_cuda();
 }
 
 int tsg_substep(tsg_handle* h, void* stream) {
@@ -667,6 +672,15 @@ int tsg_neighbors(tsg_handle* h, int32_t* counts, int32_t* list, int64_t cap, in
     cudaFree(tiles);
     int e = check_cuda();
     return rc ? rc : e;
+}
+
+int tsg_density_sum(tsg_handle* h, double* out, void* stream) {
+    if (!h || !h->sorted) return TSG_E_STATE;
+    if (!out) return TSG_E_ARG;
+    cudaStream_t s = S(stream);
+    if (use_fp32(h)) fp32_density_sum(*h->f32, out, s);
+    else { refresh_pos32_if_dirty(h, s); fp64_density_sum(h->c, h->cur, h->t, h->g, out, s); }
+    return check_cuda();
 }
 
 int tsg_reduce_diag(tsg_handle* h, double out[8], void* stream) {

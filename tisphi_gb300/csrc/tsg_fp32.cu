@@ -395,6 +395,23 @@ __global__ void __launch_bounds__(256, 6) k_corr32(K32 k, P32 p, T32 t, const fl
     });
 }
 
+// Density summation (eng/solver_sph_wc.py:30-31): sum_j mass_j W_ij over every neighbour
+// j != i, by direct traversal of the stencil (every centre sees both blocks; a utility pass,
+// not part of a step), compensated f32 sums folded every 16 neighbours, written as f64.
+template <int DIM>
+__global__ void k_density_sum32(K32 k, P32 p, const float4* __restrict__ PF, const int* __restrict__ dstart,
+                                const int* __restrict__ sstart, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    CSum sum;
+    int m = 0;
+    enum_neighbors<DIM>(k, i, p.hi, p.lo, PF, dstart, sstart, true, [&](int j, const float*, float r2) {
+        sum.add(p.mass[j] * w_pair<true, false>(k, r2).w);
+        if (++m % kFlushEvery == 0) sum.flush();
+    }, false, false);
+    out[i] = (double)sum.get();
+}
+
 __device__ __forceinline__ float tait(const K32& k, float drt, float B);
 __device__ __forceinline__ void eos_store(const K32& k, P32& p, T32& t, int i, float w, float drt, float4 v3);
 
@@ -1681,11 +1698,10 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     t.L = c.corr == 1 ? dal<float>(*st, 6 * (size_t)n) : nullptr;
     t.cnt = dal<int>(*st, n);
     t.nbr = dal<int>(*st, (size_t)k.maxn * n);
-    if (c.ti == 4) {
-        t.ddrk = dal<float>(*st, n);
-        t.dvrk = dal<float4>(*st, n);
-        if (c.solver == 3) t.dsigrk = dal<float>(*st, 6 * (size_t)n);
-    }
+    // RK4 accumulators for every integrator (substep_RK may be called on any handle)
+    t.ddrk = dal<float>(*st, n);
+    t.dvrk = dal<float4>(*st, n);
+    if (c.solver == 3) t.dsigrk = dal<float>(*st, 6 * (size_t)n);
     if (soil) {
         t.vtlo = dal<float4>(*st, n);
         t.sigt = dal<float>(*st, 6 * (size_t)n); t.dee = dal<float>(*st, n);
@@ -2633,6 +2649,15 @@ int fp32_field(Fp32State& st, const char* name, tsg_view* out, cudaStream_t s) {
 }
 
 const int* fp32_cell_start(const Fp32State& st) { return st.dstart; }
+
+void fp32_density_sum(Fp32State& st, double* out, cudaStream_t s) {
+    PhaseScope ph(s, PH_OTHER);
+    if (!st.built) fp32_sort(st, s);
+    if (st.k.dim == 2)
+        TSG_LAUNCH(k_density_sum32<2>, nblk(st.n), TPB, s, st.k, st.P[st.cur], st.pf, st.dstart, st.sstart, out);
+    else
+        TSG_LAUNCH(k_density_sum32<3>, nblk(st.n), TPB, s, st.k, st.P[st.cur], st.pf, st.dstart, st.sstart, out);
+}
 
 void fp32_neighbors(Fp32State& st, int* counts, int* offsets, int* list, cudaStream_t s) {
     const K32& k = st.k;

@@ -33,6 +33,7 @@ int fp32_field(Fp32State& st, const char* name, tsg_view* out, cudaStream_t s);
 const int* fp32_cell_start(const Fp32State& st);
 void fp32_neighbors(Fp32State& st, int* counts, int* offsets, int* list, cudaStream_t s);
 void fp32_diag(Fp32State& st, double* scratch, double* host_out8, cudaStream_t s);
+void fp32_density_sum(Fp32State& st, double* out, cudaStream_t s);
 int* fp32_err_ptr(Fp32State& st);
 // out[0] / out[1] list entries stored for the dynamic / static block, out[2] overflowed
 // particles, out[3] list builds since creation.

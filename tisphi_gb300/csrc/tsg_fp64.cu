@@ -213,6 +213,22 @@ __global__ void k_corr(Consts c, Persist64 p, Trans64 t, const int* __restrict__
     }
 }
 
+// Density summation: calc_density_task summed over for_all_neighbors
+// (eng/solver_sph_wc.py:30-31, eng/particle_system.py:259-269), sum_j mass_j W(x_i - x_j)
+// over the neighbours j != i of every particle, in traversal order.
+template <int DIM>
+__global__ void k_density_sum(Consts c, Persist64 p, Trans64 t, const int* __restrict__ cs, double* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    double xi[3];
+    load_x<DIM>(p.x, i, c.n, xi);
+    double ret = 0.0;
+    for_neighbors<DIM>(c, p.x, t.pos32, cs, i, xi, true, [&](int j, const double*, double rn) {
+        ret += p.mass[j] * kernel_W(c, rn);
+    });
+    out[i] = ret;
+}
+
 __global__ void k_init_tmp(Consts c, Persist64 p, Trans64 t) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
@@ -953,6 +969,12 @@ __global__ void k_ymax_soil(Consts c, Persist64 p, double* out) {
 void fp64_kernel_corr(const Consts& c, const Persist64& p, Trans64& t, const Grid& g, cudaStream_t s) {
     PhaseScope ph(s, PH_CORR);
     DISPATCH_DIM(c, k_corr, nblk(c.n), c, p, t, g.cell_start);
+}
+
+void fp64_density_sum(const Consts& c, const Persist64& p, const Trans64& t, const Grid& g, double* out,
+                      cudaStream_t s) {
+    PhaseScope ph(s, PH_OTHER);
+    DISPATCH_DIM(c, k_density_sum, nblk(c.n), c, p, t, g.cell_start, out);
 }
 
 void fp64_init_tmp(const Consts& c, const Persist64& p, Trans64& t, cudaStream_t s) {

@@ -134,6 +134,8 @@ void fp64_rk_update(const Consts& c, Persist64& p, Trans64& t, int m, cudaStream
 void fp64_neighbors(const Consts& c, const Persist64& p, const Trans64& t, const Grid& g,
                     int* counts, int* offsets, int* list, cudaStream_t s);
 void fp64_diag(const Consts& c, const Persist64& p, double* out8, cudaStream_t s);
+void fp64_density_sum(const Consts& c, const Persist64& p, const Trans64& t, const Grid& g, double* out,
+                      cudaStream_t s);
 void fp64_init_geostatic(const Consts& c, Persist64& p, double* scratch, cudaStream_t s);
 void fp64_refresh_pos32(const Consts& c, const Persist64& p, Trans64& t, cudaStream_t s);
 

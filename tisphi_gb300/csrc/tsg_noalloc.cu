@@ -17,7 +17,13 @@
 // each call, and calls that overlap on the GPU (different streams, no ordering between
 // them) race on it.  The first call on a device looks up the arrays' device address with
 // cudaGetSymbolAddress (once per device, with that device current); make that first call
-// before any stream capture begins.
+// before any stream capture begins.  The address is kept for the life of the process: a
+// caller that resets the device (cudaDeviceReset) must not call this entry point again in
+// that process, since the module may load at another address in the new context.
+//
+// Unlike tsg_sort, this entry point raises no status for particles outside the grid or
+// with non-finite positions: they go to the trailing bin (ascending old index), and a
+// caller counts them as cell_start[G + 1] - cell_start[G].
 #include <cstdio>
 
 #include "tsg_internal.h"
@@ -123,15 +129,76 @@ __global__ void k_na_scatter(int n, Scratch s, const int* __restrict__ cell_star
 }
 
 // Ascending old index inside every cell (the stable order of the reference's serial sort).
+// Cells of at most kSmallCell particles (every cell of an ordinary scene: a cell holds a
+// few dozen) are insertion-sorted by one thread; larger ones are left to k_na_sort_large.
+constexpr int kSmallCell = 32;
+constexpr int kMidCell = 4096;   // sorted in shared memory by one block
 __global__ void k_na_cell_sort(long long ncell, const int* __restrict__ cell_start, int* __restrict__ perm) {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     int b = cell_start[c], e = cell_start[c + 1];
+    if (e - b > kSmallCell) return;
     for (int k = b + 1; k < e; ++k) {
         int v = perm[k];
         int j = k - 1;
         while (j >= b && perm[j] > v) { perm[j + 1] = perm[j]; --j; }
         perm[j + 1] = v;
+    }
+}
+
+// Cells above kSmallCell particles (a coarse grid, or the trailing bin after particles left
+// the grid), one block per cell, grid-stride over the cells.  Up to kMidCell particles: a
+// bitonic sort of the cell's entries in shared memory.  Above: the cell's entries are
+// rebuilt in ascending order from a block-wide scan over every particle of the flag
+// "cell_of[i] == c" (n / TPB trips; at most n / kMidCell cells are that large).
+__global__ void __launch_bounds__(TPB) k_na_sort_large(long long ncell, const int* __restrict__ cell_start,
+                                                       const int* __restrict__ cell_of, int n,
+                                                       int* __restrict__ perm) {
+    __shared__ int buf[kMidCell];
+    __shared__ int warp_tot[TPB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (long long c = blockIdx.x; c < ncell; c += gridDim.x) {
+        const int b = cell_start[c], e = cell_start[c + 1], m = e - b;
+        if (m <= kSmallCell) continue;  // uniform across the block
+        if (m <= kMidCell) {
+            int p2 = 1;
+            while (p2 < m) p2 <<= 1;
+            for (int k = threadIdx.x; k < p2; k += TPB) buf[k] = k < m ? perm[b + k] : 0x7fffffff;
+            __syncthreads();
+            for (int size = 2; size <= p2; size <<= 1) {
+                for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                    for (int k = threadIdx.x; k < p2; k += TPB) {
+                        const int o = k ^ stride;
+                        if (o > k) {
+                            const bool up = (k & size) == 0;
+                            const int a = buf[k], z = buf[o];
+                            if ((a > z) == up) { buf[k] = z; buf[o] = a; }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            for (int k = threadIdx.x; k < m; k += TPB) perm[b + k] = buf[k];
+            __syncthreads();
+        } else {
+            int base = 0;
+            for (int i0 = 0; i0 < n; i0 += TPB) {
+                const int i = i0 + threadIdx.x;
+                const int f = (i < n && cell_of[i] == (int)c) ? 1 : 0;
+                const unsigned bal = __ballot_sync(0xffffffffu, f);
+                const int before_lane = __popc(bal & ((1u << lane) - 1u));
+                if (lane == 0) warp_tot[wid] = __popc(bal);
+                __syncthreads();
+                int before = 0, total = 0;
+                for (int w = 0; w < TPB / 32; ++w) {
+                    if (w < wid) before += warp_tot[w];
+                    total += warp_tot[w];
+                }
+                if (f) perm[b + base + before + before_lane] = i;
+                base += total;
+                __syncthreads();
+            }
+        }
     }
 }
 
@@ -159,6 +226,7 @@ extern "C" int tsg_sort_noalloc(const tsg_config* cfg, const double* x, int64_t 
     TSG_LAUNCH(k_na_scan, 1, TPB, st, s.counts, m, cell_start);
     TSG_LAUNCH(k_na_scatter, (nn + TPB - 1) / TPB, TPB, st, nn, s, cell_start, perm);
     TSG_LAUNCH(k_na_cell_sort, (m + TPB - 1) / TPB, TPB, st, (long long)m, cell_start, perm);
+    TSG_LAUNCH(k_na_sort_large, 152, TPB, st, (long long)m, cell_start, s.cell_of, nn, perm);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         std::fprintf(stderr, "tisphi_gb300: CUDA error: %s\n", cudaGetErrorString(e));

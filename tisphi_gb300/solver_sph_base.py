@@ -80,11 +80,19 @@ class SPHBase:
         self.one_step()
         self.advect_LF()
 
-    def substep_RK(self):
-        self._call("tsg_substep") if self.flagTI == 4 else self._rk_manual()
+    def update_RK(self, m):
+        self._call("tsg_rk_update", int(m))
 
-    def _rk_manual(self):
-        raise NotImplementedError("RK4 substeps need timeIntegration = 4 at construction")
+    def substep_RK(self):
+        """The reference's RK4 sequence (eng/solver_sph_base.py:172-180), on a handle of any
+        integrator: every handle holds the RK accumulators."""
+        self.init_RK()
+        for q, m in enumerate((1, 2, 2, 1)):
+            self.one_step()
+            self.update_RK(m)
+            if q < 3:
+                self.advect_RK_4()
+        self.advect_RK()
 
     def advect_pos(self):
         self._call("tsg_advect", nat.TSG_ADVECT_POS)
