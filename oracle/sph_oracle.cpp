@@ -106,6 +106,53 @@ inline double powi(double x, long n) {  // binary exponentiation, low bit first
     return r;
 }
 
+// Orthogonal polar factor of a 3x3 matrix: Higham's scaled Newton iteration
+// X <- (g X + X^-T / g) / 2 with g = (|X^-1|_F / |X|_F)^(1/2) (N. J. Higham, "Computing the
+// polar decomposition - with applications", SIAM J. Sci. Stat. Comput. 7, 1986), X^-T from
+// the cofactors, until an update changes X by at most 1e-14 (Frobenius) or after 60 steps.
+// A matrix whose third row and column are zero (a 2D body: every z offset is zero) gets
+// A[2][2] = 1 first, so the z axis maps to itself; a singular matrix gives the identity.
+inline M3 polar3(const M3& A) {
+    M3 X = A;
+    if (X.m[0][2] == 0.0 && X.m[1][2] == 0.0 && X.m[2][0] == 0.0 && X.m[2][1] == 0.0 && X.m[2][2] == 0.0)
+        X.m[2][2] = 1.0;
+    for (int it = 0; it < 60; ++it) {
+        const double (*x)[3] = X.m;
+        double c[3][3];
+        c[0][0] = x[1][1] * x[2][2] - x[1][2] * x[2][1];
+        c[0][1] = x[1][2] * x[2][0] - x[1][0] * x[2][2];
+        c[0][2] = x[1][0] * x[2][1] - x[1][1] * x[2][0];
+        c[1][0] = x[0][2] * x[2][1] - x[0][1] * x[2][2];
+        c[1][1] = x[0][0] * x[2][2] - x[0][2] * x[2][0];
+        c[1][2] = x[0][1] * x[2][0] - x[0][0] * x[2][1];
+        c[2][0] = x[0][1] * x[1][2] - x[0][2] * x[1][1];
+        c[2][1] = x[0][2] * x[1][0] - x[0][0] * x[1][2];
+        c[2][2] = x[0][0] * x[1][1] - x[0][1] * x[1][0];
+        const double det = (x[0][0] * c[0][0] + x[0][1] * c[0][1]) + x[0][2] * c[0][2];
+        if (det == 0.0 || !std::isfinite(det)) return meye();
+        double fx = 0.0, fy = 0.0;
+        double y[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                y[a][b] = c[a][b] / det;
+                fx += x[a][b] * x[a][b];
+                fy += y[a][b] * y[a][b];
+            }
+        const double gm = std::sqrt(std::sqrt(fy) / std::sqrt(fx));
+        double ch = 0.0;
+        M3 Xn;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                Xn.m[a][b] = 0.5 * (gm * x[a][b] + y[a][b] / gm);
+                const double d = Xn.m[a][b] - x[a][b];
+                ch += d * d;
+            }
+        X = Xn;
+        if (ch <= 1e-28) break;
+    }
+    return X;
+}
+
 // Particle record: the fields of eng/particle_func.py:10-88 that the path reads or writes.
 struct P {
     int obj_id, mat_id, mat_type, is_dynamic;
@@ -144,6 +191,11 @@ struct Sys {
     double damp_E = 0;
     double g[3];
     double vsound = 0;
+    // dynamic rigid bodies (eng/solver_sph_base.py:467-518): object ids and rest centres of
+    // mass, computed at creation from the input positions in input order
+    int n_rigid_dyn = 0;
+    std::vector<int> rigid_ids;
+    std::vector<V3> rigid_rest_cm;
 
     bool is_fluid(int p) const { return pt[p].mat_type == MAT_FLUID; }
     bool is_soil(int p) const { return pt[p].mat_type == MAT_SOIL; }
@@ -383,21 +435,7 @@ struct Sys {
                 });
                 pt[i].d_density = dd * pt[i].density_tmp;
                 V3 dv = vzero();
-                for_all_neighbors(i, [&](int j) {
-                    V3 xij = vsub(pt[i].x, pt[j].x);
-                    V3 visc = vzero();
-                    double xn = vnorm(xij);
-                    if (is_fluid(j)) {
-                        double c = visc_fac * pt[j].m_V * std::min(vdot(vsub(pt[i].v_tmp, pt[j].v_tmp), xij), 0.0) / (xn * xn + eps_h2);
-                        visc = vscale(c, dW(xij));
-                    } else if (is_bdy(j) || is_rigid(j)) {
-                        double c = visc_fac * pt[j].m_V * rho0 / pt[i].density_tmp * std::min(vdot(vsub(pt[i].v_tmp, pt[j].v_tmp), xij), 0.0) / (xn * xn + eps_h2);
-                        visc = vscale(c, dW(xij));
-                    }
-                    double cp = -rho0 * pt[j].m_V * (pt[i].pressure / (pt[i].density_tmp * pt[i].density_tmp) + pt[j].pressure / (pt[j].density_tmp * pt[j].density_tmp));
-                    V3 press = vscale(cp, dW(xij));
-                    dv = vadd(dv, vadd(visc, press));
-                });
+                for_all_neighbors(i, [&](int j) { dv = vadd(dv, wc_force_pair(i, j)); });
                 if (rep_on()) {
                     for_all_neighbors(i, [&](int j) {
                         if (is_rep(j)) dv = vadd(dv, rep_force(vsub(pt[i].x, pt[j].x)));
@@ -406,6 +444,46 @@ struct Sys {
                 pt[i].d_vel = vadd(dv, v3(g[0], g[1], g[2]));
             }
             if (is_rigid_static(i)) pt[i].d_vel = vzero();
+        }
+        if (n_rigid_dyn) rigid_reaction();
+    }
+
+    // One neighbour's term of calc_d_vel_task (eng/solver_sph_wc.py:34-71):
+    // tmp = viscosity_force(i, j) + pressure_force(i, j).
+    V3 wc_force_pair(int i, int j) const {
+        const double rho0 = prm.density0;
+        V3 xij = vsub(pt[i].x, pt[j].x);
+        V3 visc = vzero();
+        double xn = vnorm(xij);
+        if (is_fluid(j)) {
+            double c = visc_fac * pt[j].m_V * std::min(vdot(vsub(pt[i].v_tmp, pt[j].v_tmp), xij), 0.0) / (xn * xn + eps_h2);
+            visc = vscale(c, dW(xij));
+        } else if (is_bdy(j) || is_rigid(j)) {
+            double c = visc_fac * pt[j].m_V * rho0 / pt[i].density_tmp * std::min(vdot(vsub(pt[i].v_tmp, pt[j].v_tmp), xij), 0.0) / (xn * xn + eps_h2);
+            visc = vscale(c, dW(xij));
+        }
+        double cp = -rho0 * pt[j].m_V * (pt[i].pressure / (pt[i].density_tmp * pt[i].density_tmp) + pt[j].pressure / (pt[j].density_tmp * pt[j].density_tmp));
+        V3 press = vscale(cp, dW(xij));
+        return vadd(visc, press);
+    }
+
+    // The reaction on dynamic rigid particles: the reference subtracts each flow particle's
+    // pair term from its dynamic rigid neighbour inside the flow particle's loop
+    // (`pt[j].d_vel -= tmp`, eng/solver_sph_wc.py:70-71, eng/solver_sph_muI.py:45-46,
+    // eng/solver_sph_dp.py:164-165), an unsynchronised scatter.  Serially, rigid particle j
+    // receives the terms of its flow neighbours i in ascending i, which is the order of j's
+    // own neighbour traversal (cells in increasing flattened index, particles ascending):
+    // here each j gathers them in that order, starting from the g its first loop set.
+    void rigid_reaction() {
+        #pragma omp parallel for schedule(dynamic, 64)
+        for (int j = 0; j < n; ++j) {
+            if (!is_rigid_dynamic(j)) continue;
+            V3 d = pt[j].d_vel;
+            for_all_neighbors(j, [&](int i) {
+                if (prm.solver == 1 ? is_fluid(i) : is_soil(i))
+                    d = vsub(d, prm.solver == 1 ? wc_force_pair(i, j) : stress_div_pair(i, j));
+            });
+            pt[j].d_vel = d;
         }
     }
 
@@ -426,18 +504,21 @@ struct Sys {
         });
         return r;
     }
-    V3 stress_div_sum(int i) const {  // calc_d_vel_from_stress_task (eng/solver_sph_muI.py:39-46)
+    // One neighbour's term of calc_d_vel_from_stress_task (eng/solver_sph_muI.py:39-46,
+    // eng/solver_sph_dp.py:157-165): tmp = m_Vj rho~_j (s~_j / rho~_j^2 + s~_i / rho~_i^2) grad~W_ij.
+    V3 stress_div_pair(int i, int j) const {
+        double rj2 = pt[j].density_tmp * pt[j].density_tmp;
+        double ri2 = pt[i].density_tmp * pt[i].density_tmp;
+        M3 M;
+        for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q)
+                M.m[p][q] = (pt[j].stress_tmp.m[p][q] / rj2 + pt[i].stress_tmp.m[p][q] / ri2) + 0.0 * (p == q ? 1.0 : 0.0);
+        M3 S = mscale(pt[j].m_V * pt[j].density_tmp, M);
+        return matvec(S, dW_corr(i, j));
+    }
+    V3 stress_div_sum(int i) const {  // calc_d_vel_from_stress_task summed over the neighbours
         V3 r = vzero();
-        for_all_neighbors(i, [&](int j) {
-            double rj2 = pt[j].density_tmp * pt[j].density_tmp;
-            double ri2 = pt[i].density_tmp * pt[i].density_tmp;
-            M3 M;
-            for (int p = 0; p < 3; ++p)
-                for (int q = 0; q < 3; ++q)
-                    M.m[p][q] = (pt[j].stress_tmp.m[p][q] / rj2 + pt[i].stress_tmp.m[p][q] / ri2) + 0.0 * (p == q ? 1.0 : 0.0);
-            M3 S = mscale(pt[j].m_V * pt[j].density_tmp, M);
-            r = vadd(r, matvec(S, dW_corr(i, j)));
-        });
+        for_all_neighbors(i, [&](int j) { r = vadd(r, stress_div_pair(i, j)); });
         return r;
     }
     V3 damping(int i) const {  // calc_viscous_damping (eng/solver_sph_base.py:714-715)
@@ -500,6 +581,7 @@ struct Sys {
         #pragma omp parallel for
         for (int i = 0; i < n; ++i)
             if (is_rigid_static(i)) pt[i].d_vel = vzero();
+        if (n_rigid_dyn) rigid_reaction();
     }
 
     // ---- Drucker-Prager pieces (eng/solver_sph_dp.py:42-208) ----
@@ -599,6 +681,7 @@ struct Sys {
         #pragma omp parallel for
         for (int i = 0; i < n; ++i)
             if (is_rigid_static(i)) pt[i].d_vel = vzero();
+        if (n_rigid_dyn) rigid_reaction();
     }
 
     void one_step() {
@@ -797,7 +880,56 @@ struct Sys {
         substep();
         advect_pos();
         advect_something();
+        if (n_rigid_dyn) solve_rigid_body();
         enforce_boundary();
+    }
+
+    // calc_cm (eng/solver_sph_base.py:502-511): mass-weighted mean position of object o's
+    // dynamic rigid particles, summed in particle order.
+    V3 rigid_cm(int o) const {
+        double sum_m = 0.0;
+        V3 cm = vzero();
+        for (int i = 0; i < n; ++i) {
+            if (!(is_rigid_dynamic(i) && pt[i].obj_id == o)) continue;
+            cm = vadd(cm, vscale(pt[i].mass, pt[i].x));
+            sum_m += pt[i].mass;
+        }
+        return v3(cm.c[0] / sum_m, cm.c[1] / sum_m, cm.c[2] / sum_m);
+    }
+
+    // solve_rigid_body / solve_constraints (eng/solver_sph_base.py:472-500): shape matching
+    // of every dynamic rigid object.  A = sum m_V rho ((p) (x) q) with p = x - cm,
+    // q = x0 - rest cm (the reference's m_V * density * p @ q.T, scalar products first),
+    // R the orthogonal polar factor of A (polar3: the reference calls ti.polar_decompose,
+    // whose algorithm lives in Taichi; this is Higham's scaled Newton iteration), identity when
+    // every entry of R is below 1e-8; then x += (cm + R q) - x.
+    void solve_rigid_body() {
+        for (size_t k = 0; k < rigid_ids.size(); ++k) {
+            const int o = rigid_ids[k];
+            const V3 cm = rigid_cm(o);
+            M3 A = mzero();
+            for (int i = 0; i < n; ++i) {
+                if (!(is_rigid_dynamic(i) && pt[i].obj_id == o)) continue;
+                const V3 q = vsub(pt[i].x0, rigid_rest_cm[k]);
+                const V3 pp = vsub(pt[i].x, cm);
+                const double s = pt[i].m_V * pt[i].density;
+                const V3 sp = vscale(s, pp);
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) A.m[a][b] = A.m[a][b] + sp.c[a] * q.c[b];
+            }
+            M3 R = polar3(A);
+            bool small = true;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) small = small && std::fabs(R.m[a][b]) < EPS;
+            if (small) R = meye();
+            #pragma omp parallel for
+            for (int i = 0; i < n; ++i) {
+                if (!(is_rigid_dynamic(i) && pt[i].obj_id == o)) continue;
+                const V3 goal = vadd(cm, matvec(R, vsub(pt[i].x0, rigid_rest_cm[k])));
+                const V3 corr = vscale(1.0, vsub(goal, pt[i].x));
+                pt[i].x = vadd(pt[i].x, corr);
+            }
+        }
     }
 
     void init_stress_geostatic() {  // eng/solver_sph_base.py:249-260
@@ -875,6 +1007,16 @@ void* orc_create(const orc_params* prm, int n, const double* x, const double* v,
     }
     s->damp_E = prm->E;
     if (prm->solver == 3 && prm->init_geostatic) s->init_stress_geostatic();
+    // init_rigid_body (eng/solver_sph_base.py:467-470): rest centre of mass of every dynamic
+    // rigid object, from the input positions
+    for (int i = 0; i < n; ++i) {
+        if (!s->is_rigid_dynamic(i)) continue;
+        ++s->n_rigid_dyn;
+        if (std::find(s->rigid_ids.begin(), s->rigid_ids.end(), s->pt[i].obj_id) == s->rigid_ids.end())
+            s->rigid_ids.push_back(s->pt[i].obj_id);
+    }
+    std::sort(s->rigid_ids.begin(), s->rigid_ids.end());
+    for (int o : s->rigid_ids) s->rigid_rest_cm.push_back(s->rigid_cm(o));
     return s;
 }
 

@@ -1,9 +1,9 @@
 """Generate golden vectors by running the reference's own source (Rabmelon/tiSPHi, eng/*.py)
 under the serial Taichi-API emulator in tests/golden/taichi_emul.
 
-Run in a checkout that has the reference mounted (default /root/reference):
+Run with a checkout of the reference (its eng/ package on the path):
 
-    python tests/golden/make_golden.py [--reference PATH]
+    python tests/golden/make_golden.py --reference PATH   (or TISPHI_REFERENCE=PATH)
 
 Each case builds a scene dict (tisphi_gb300.scenes), writes it to a temporary JSON file,
 constructs the reference's ``Simulation`` from that file, runs ``solver.step()`` a few
@@ -47,6 +47,9 @@ def cases():
                                   seed=14), 2),
         "dp2d_lf_xsph": (scenes.column_2d(method=3, spacing=0.01, width=0.1, height=0.05, domain=(0.2, 0.1),
                                           seed=15, integration=2, xsph=True), 2),
+        # dynamic rigid box on the water surface: the reaction scatter and shape matching
+        "wc2d_rigid": (scenes.floating_box_2d(spacing=0.04, water=(0.4, 0.2), box=(0.12, 0.08), box_at=(0.12, 0.2),
+                                              domain=(0.8, 0.6), jitter=4e-4, seed=16), 3),
     }
 
 
@@ -152,9 +155,12 @@ def run_case(name, scene, steps, out_dir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("TISPHI_REFERENCE"),
+                    help="checkout of the reference (or set TISPHI_REFERENCE)")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("--reference PATH (or TISPHI_REFERENCE) is required")
     sys.dont_write_bytecode = True
     sys.path.insert(0, os.path.join(HERE, "taichi_emul"))
     sys.path.insert(1, args.reference)

@@ -185,6 +185,11 @@ class Mat:
                 out[r, c] = s
         return Mat(out)
 
+    def __bool__(self):
+        # all(mat) in a Taichi kernel is the elementwise all; Python's all() iterates the
+        # rows and takes each row's truth value: all of its elements
+        return bool(np.all(self.a != 0))
+
     def __iter__(self):
         if self._vec():
             return iter([v.item() for v in self.a[:, 0]])
@@ -448,7 +453,58 @@ def random(dtype=float):
 
 
 def polar_decompose(A):
-    raise NotImplementedError("rigid bodies are outside the emulated subset")
+    """(R, S) with R the orthogonal polar factor of the 3x3 matrix A and S = R^T A.
+
+    Taichi's own routine is not available here; the emulator uses the algorithm the oracle
+    and the CUDA forms restate, in the same operation order (Python floats are IEEE f64):
+    Higham's scaled Newton iteration X <- (g X + X^-T / g) / 2, g = (|X^-1|_F / |X|_F)^(1/2),
+    X^-T from the cofactors, until an update changes X by at most 1e-14 (Frobenius) or after
+    60 steps; a zero third row and column (2D body) gets A[2][2] = 1 first; a singular
+    matrix gives the identity."""
+    a = A.a.astype(np.float64)
+    x = [[float(a[r, c]) for c in range(3)] for r in range(3)]
+    if x[0][2] == 0.0 and x[1][2] == 0.0 and x[2][0] == 0.0 and x[2][1] == 0.0 and x[2][2] == 0.0:
+        x[2][2] = 1.0
+    eye = [[1.0 if r == c else 0.0 for c in range(3)] for r in range(3)]
+    R = None
+    for _ in range(60):
+        c = [[0.0] * 3 for _ in range(3)]
+        c[0][0] = x[1][1] * x[2][2] - x[1][2] * x[2][1]
+        c[0][1] = x[1][2] * x[2][0] - x[1][0] * x[2][2]
+        c[0][2] = x[1][0] * x[2][1] - x[1][1] * x[2][0]
+        c[1][0] = x[0][2] * x[2][1] - x[0][1] * x[2][2]
+        c[1][1] = x[0][0] * x[2][2] - x[0][2] * x[2][0]
+        c[1][2] = x[0][1] * x[2][0] - x[0][0] * x[2][1]
+        c[2][0] = x[0][1] * x[1][2] - x[0][2] * x[1][1]
+        c[2][1] = x[0][2] * x[1][0] - x[0][0] * x[1][2]
+        c[2][2] = x[0][0] * x[1][1] - x[0][1] * x[1][0]
+        det = (x[0][0] * c[0][0] + x[0][1] * c[0][1]) + x[0][2] * c[0][2]
+        if det == 0.0 or not _m.isfinite(det):
+            R = eye
+            break
+        fx = 0.0
+        fy = 0.0
+        y = [[0.0] * 3 for _ in range(3)]
+        for r in range(3):
+            for k in range(3):
+                y[r][k] = c[r][k] / det
+                fx += x[r][k] * x[r][k]
+                fy += y[r][k] * y[r][k]
+        gm = _m.sqrt(_m.sqrt(fy) / _m.sqrt(fx))
+        ch = 0.0
+        xn = [[0.0] * 3 for _ in range(3)]
+        for r in range(3):
+            for k in range(3):
+                xn[r][k] = 0.5 * (gm * x[r][k] + y[r][k] / gm)
+                d = xn[r][k] - x[r][k]
+                ch += d * d
+        x = xn
+        if ch <= 1e-28:
+            break
+    if R is None:
+        R = x
+    Rm = Mat(np.array(R, dtype=np.float64))
+    return Rm, Rm.transpose() @ A
 
 
 # ---------------------------------------------------------------- fields

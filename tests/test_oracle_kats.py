@@ -269,3 +269,49 @@ def test_density_sum_matches_brute_force(oracle_lib, dim, kernel):
         mid = (mt == 1) & (np.abs(xs[:, 0] - 0.3) < 0.05) & (np.abs(xs[:, 1] - 0.2) < 0.05)
         assert mid.any()
         np.testing.assert_allclose(rho[mid], expect, rtol=1e-9)
+
+
+def test_rigid_free_fall_and_polar(oracle_lib):
+    """Dynamic rigid bodies in the oracle (eng/solver_sph_base.py:467-518): a box released
+    above the water, out of reach of any flow particle, falls with gravity alone (leap-frog:
+    v = N g dt, x = x0 + g dt^2 N (N + 1) / 2) and keeps its shape; the shape-matching
+    rotation of a pure translation is the identity.  The polar factor of the emulator's
+    ti.polar_decompose (the algorithm the oracle and the CUDA forms restate) equals U V^T of
+    numpy's SVD for well-conditioned matrices, and maps the z axis to itself for a 2D body."""
+    import os
+    import sys
+    d = scenes.floating_box_2d(box_at=(0.8, 0.6), box=(0.12, 0.08), jitter=0.0)
+    orc = oracle_lib.OracleSim(cfg_of(d))
+    N, dt, g = 120, orc.params.dt, -9.81
+    orc.step(N)
+    mt = orc.get("mat_type")
+    ids = orc.get("id0")[mt == 11].astype(np.int64)
+    x0 = orc.scene.x[ids]
+    xr, vr = orc.get("x")[mt == 11], orc.get("v")[mt == 11]
+    np.testing.assert_allclose(vr[:, 1], N * g * dt, rtol=1e-12)
+    np.testing.assert_allclose(xr[:, 1] - x0[:, 1], g * dt * dt * N * (N + 1) / 2, rtol=1e-9)
+    np.testing.assert_allclose(xr[:, 0], x0[:, 0], atol=1e-12)
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden", "taichi_emul"))
+    try:
+        import taichi as ti_emul
+    finally:
+        sys.path.pop(0)
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        if np.linalg.det(q) < 0:
+            q[:, 0] = -q[:, 0]
+        a = rng.normal(size=(3, 3))
+        spd = a @ a.T + 3.0 * np.eye(3)
+        A = (q @ spd) * 10.0 ** rng.uniform(-4, 4)
+        R, S = ti_emul.polar_decompose(ti_emul.Matrix(A))
+        u, _, vt = np.linalg.svd(A)
+        np.testing.assert_allclose(R.a, u @ vt, atol=1e-12)
+        np.testing.assert_allclose(R.a @ S.a, A, rtol=1e-10, atol=1e-12 * np.abs(A).max())
+    th = 0.3
+    A2 = np.zeros((3, 3))
+    A2[:2, :2] = np.array([[np.cos(th), -np.sin(th)], [np.sin(th), np.cos(th)]]) @ np.array([[2.0, 0.5], [0.5, 1.0]])
+    R2, _ = ti_emul.polar_decompose(ti_emul.Matrix(A2))
+    np.testing.assert_allclose(R2.a[:2, :2], [[np.cos(th), -np.sin(th)], [np.sin(th), np.cos(th)]], atol=1e-12)
+    assert R2.a[2, 2] == 1.0 and not np.any(R2.a[2, :2]) and not np.any(R2.a[:2, 2])

@@ -84,6 +84,32 @@ def column_2d(method=3, spacing=0.001, dt=1e-5, jitter_frac=0.01, seed=3, integr
     }
 
 
+def floating_box_2d(spacing=0.02, dt=1e-4, jitter=2e-4, seed=5, integration=2, box_density=500.0,
+                    box=(0.12, 0.08), box_at=(0.24, 0.4), water=(0.6, 0.4), domain=(1.2, 0.8), xsph=False, corr=0):
+    """A 2D water column with a dynamic rigid box resting on its surface: the box (shape
+    matching, eng/solver_sph_base.py:467-518) feels the water's pressure and viscous
+    reaction and gravity; rigid material type 11, isDynamic true."""
+    d = dambreak_2d(spacing=spacing, width=water[0], height=water[1], dt=dt, jitter=jitter, seed=seed,
+                    integration=integration, domain=domain, xsph=xsph, corr=corr)
+    d["Materials"].append({"matId": 1, "matType": 11, "color": [155, 55, 55], "density0": box_density})
+    b = block((box[0], box[1], 0.05), translation=(box_at[0], box_at[1], 0.0), material=1, obj=1)
+    b["isDynamic"] = True
+    d["Blocks"].append(b)
+    return d
+
+
+def floating_box_3d(spacing=0.02, dt=2e-5, jitter_frac=0.01, seed=6, integration=2, box_density=500.0, corr=1):
+    """The 3D counterpart of floating_box_2d: water 0.3 x 0.2 x 0.16 m in a 0.6 x 0.4 x 0.2 m
+    domain, a 0.1 x 0.06 x 0.08 m dynamic rigid box on the surface."""
+    d = dambreak_3d(spacing=spacing, dt=dt, jitter_frac=jitter_frac, seed=seed, corr=corr, integration=integration,
+                    domain=(0.6, 0.4, 0.2), size=(0.3, 0.2, 0.16))
+    d["Materials"].append({"matId": 1, "matType": 11, "color": [155, 55, 55], "density0": box_density})
+    b = block((0.1, 0.06, 0.08), translation=(0.1, 0.2, 0.04), material=1, obj=1)
+    b["isDynamic"] = True
+    d["Blocks"].append(b)
+    return d
+
+
 def dambreak_ensemble(n=256, seed=7, spacing=0.01, dt=1e-4, width=(0.3, 1.5), height=(0.2, 0.8),
                       stiffness=(2e4, 1e5), viscosity=(1e-3, 1e-2), domain=(3.22, 1.6), jitter=1e-4):
     """Scene dicts of an ensemble of 2D dambreaks with seeded block sizes and fluid parameters."""
