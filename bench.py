@@ -527,6 +527,11 @@ def run_ours(args):
             "energy_change_rel": {"fp32_mixed": c32["energy_rel"], "fp64": c64["energy_rel"]},
             "momentum_change": {"fp32_mixed": c32["momentum_change"], "fp64": c64["momentum_change"]},
             "mass_rel": {"fp32_mixed": c32["mass_rel"], "fp64": c64["mass_rel"]}}
+    # the other forms' headline checks, bounded: the 256-scene ensemble against sequential
+    # launches, and short adjoint-vs-finite-difference checks (N = 1)
+    if rank == 0 and ws == 1 and args.workload == "3d" and not args.no_forms:
+        line["ensemble"] = ensemble_report(256, steps=20, warmup=3, seq_steps=5, tune=False)
+        line["adjoint_check"] = adjoint_check()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cfg_dict)
     if rank == 0:
@@ -535,32 +540,30 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_batch(args):
-    """256-scene dambreak ensemble: one batched handle (graph replays, autotuned launch shape)
-    against the same scenes stepped one after another through their own handles."""
+def ensemble_report(nscenes=256, steps=20, warmup=3, seq_steps=10, tune=True):
+    """The 256-scene dambreak ensemble: one batched handle (graph replays, autotuned launch
+    shape) against the same scenes stepped one after another through their own handles."""
     import torch
-    if not torch.cuda.is_available():
-        raise SystemExit("bench.py needs a CUDA GPU")
-    from tisphi_gb300 import build_native, scenes
-    build_native.build()
+
+    from tisphi_gb300 import scenes
     from tisphi_gb300.batch import SceneBatch
     from tisphi_gb300.configer_builder import SimConfiger
     from tisphi_gb300.simulation import Simulation
-    cfgs = scenes.dambreak_ensemble(args.scenes)
+    cfgs = scenes.dambreak_ensemble(nscenes)
     batch = SceneBatch(cfgs)
     nf = int(batch.n_fluid.sum())
-    tuned = batch.autotune(trial_steps=10)
+    tuned = batch.autotune(trial_steps=10) if tune else None
     stream = torch.cuda.current_stream()
-    batch.step(args.warmup)
+    batch.step(warmup)
     torch.cuda.synchronize()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(torch.cuda.current_device()) as clk:
         torch.cuda.synchronize()
         start.record(stream)
-        batch.step(args.steps)
+        batch.step(steps)
         stop.record(stream)
         torch.cuda.synchronize()
-    ms = start.elapsed_time(stop) / args.steps
+    ms = start.elapsed_time(stop) / steps
     batch.check_errors()
     stats = batch.list_stats()
     del batch
@@ -569,26 +572,88 @@ def run_batch(args):
     for s in sims:
         s.solver.step(1)
     torch.cuda.synchronize()
-    k_seq = max(1, min(args.steps, 10))
+    k_seq = max(1, min(steps, seq_steps))
     start.record(stream)
     for s in sims:
         s.solver.step(k_seq)
     stop.record(stream)
     torch.cuda.synchronize()
     ms_seq = start.elapsed_time(stop) / k_seq
+    del sims
+    torch.cuda.synchronize()
+    return {"scenes": nscenes, "n_fluid": nf, "ms_per_step": ms, "value": nscenes / (ms * 1e-3),
+            "unit": "scenes*steps/s", "steps": steps, "warmup": warmup, "launch": tuned,
+            "particle_updates_per_s": nf / (ms * 1e-3),
+            "sequential": {"ms_per_step_all_scenes": ms_seq, "value": nscenes / (ms_seq * 1e-3),
+                           "steps_timed": k_seq, "how": "each scene's own FP32-mixed handle, stepped in turn"},
+            "speedup_vs_sequential": ms_seq / ms, "lists": stats, "clocks": clk.summary()}
+
+
+def run_batch(args):
+    """256-scene dambreak ensemble, batched vs sequential (ensemble_report)."""
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    from tisphi_gb300 import build_native
+    build_native.build()
+    rep = ensemble_report(args.scenes, args.steps, args.warmup)
     line = {"metric": "scenes*steps/s, 256-scene 2D WCSPH dambreak ensemble, batched vs sequential",
-            "value": args.scenes / (ms * 1e-3), "unit": "scenes*steps/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "value": rep["value"], "unit": "scenes*steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": rep["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"{args.scenes} 2D WCSPH dambreaks, spacing 0.01 m, block width U[0.3, 1.5] m, "
                                    f"height U[0.2, 0.8] m, B log-U[2e4, 1e5], nu log-U[1e-3, 1e-2], seed 7, "
-                                   f"LF dt 1e-4", "n_fluid": nf,
+                                   f"LF dt 1e-4", "n_fluid": rep["n_fluid"],
                        "l2": "working set ~0.15 GB > 129 MB L2 (no flush)"},
-            "launch": tuned, "particle_updates_per_s": nf / (ms * 1e-3),
-            "sequential": {"ms_per_step_all_scenes": ms_seq, "value": args.scenes / (ms_seq * 1e-3),
-                           "steps_timed": k_seq, "how": "each scene's own FP32-mixed handle, stepped in turn"},
-            "speedup_vs_sequential": ms_seq / ms, "lists": stats, "clocks": clk.summary()}
+            **{k: rep[k] for k in ("launch", "particle_updates_per_s", "sequential", "speedup_vs_sequential",
+                                   "lists", "clocks")}}
     print(json.dumps(line))
+
+
+def adjoint_check():
+    """Short adjoint checks against central finite differences of the FP64 form: the
+    differentiable mu(I) column (0.2 x 0.1 m at spacing 0.002 m, symplectic Euler at dt 2e-5)
+    over 200 steps (friction angle), and the 2D WCSPH dambreak (spacing 0.01 m, 0.6 x 0.4 m
+    block, symplectic Euler at dt 1e-4) over 400 steps (stiffness and viscosity)."""
+    import torch
+
+    from tisphi_gb300 import scenes
+    from tisphi_gb300.adjoint import MuIRollout, WCRollout, distal_loss, rollout_positions
+    t0 = time.perf_counter()
+    d = scenes.column_2d(method=2, spacing=0.002, dt=2e-5)
+    model = MuIRollout(d, nsteps=200, checkpoint_every=100)
+    params = torch.tensor([21.9, 0.0], dtype=torch.float64, requires_grad=True)
+    loss, sel = distal_loss(model(params))
+    loss.backward()
+    g = params.grad.tolist()
+    delta = 1e-4
+    l_hi, _ = distal_loss(rollout_positions(d, 200, 21.9 + delta, 0.0), sel=sel)
+    l_lo, _ = distal_loss(rollout_positions(d, 200, 21.9 - delta, 0.0), sel=sel)
+    fd = (float(l_hi) - float(l_lo)) / (2 * delta)
+    mui = {"steps": 200, "n_particles": model.n, "grad_friction_deg": g[0], "fd_friction_deg": fd,
+           "rel_err": abs(g[0] - fd) / abs(fd)}
+    dw = scenes.dambreak_2d(spacing=0.01, width=0.6, height=0.4, domain=(1.2, 0.8), integration=1)
+    mw = WCRollout(dw, nsteps=400, checkpoint_every=100)
+    B0, nu0 = mw.stiffness, mw.viscosity
+    pw = torch.tensor([B0, nu0], dtype=torch.float64, requires_grad=True)
+    lw, selw = distal_loss(mw(pw), target=0.7)
+    lw.backward()
+    gw = pw.grad.tolist()
+    fdw = []
+    for k in range(2):
+        lo, hi = [B0, nu0], [B0, nu0]
+        dk = 1e-4 * (B0, nu0)[k]
+        lo[k] -= dk
+        hi[k] += dk
+        a, _ = distal_loss(rollout_positions(dw, 400, *hi), target=0.7, sel=selw)
+        b, _ = distal_loss(rollout_positions(dw, 400, *lo), target=0.7, sel=selw)
+        fdw.append((float(a) - float(b)) / (2 * dk))
+    wc = {"steps": 400, "n_particles": mw.n, "grad": {"stiffness": gw[0], "viscosity": gw[1]},
+          "fd": {"stiffness": fdw[0], "viscosity": fdw[1]},
+          "rel_err": {"stiffness": abs(gw[0] - fdw[0]) / abs(fdw[0]), "viscosity": abs(gw[1] - fdw[1]) / abs(fdw[1])}}
+    torch.cuda.synchronize()
+    return {"against": "central finite differences of the FP64 form, relative step 1e-4",
+            "mui_column": mui, "wcsph_dambreak": wc, "wall_s": time.perf_counter() - t0}
 
 
 def run_adjoint(args):
@@ -872,6 +937,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-full-run", action="store_true", help="skip the 1,000-step FP32-mixed run")
     ap.add_argument("--no-errors", action="store_true", help="skip the FP32-mixed vs FP64 error report")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the ensemble and adjoint checks of the default line")
     ap.add_argument("--error-steps", type=int, default=1000,
                     help="length of the FP32-mixed vs FP64 comparison of the default workload (N = 1)")
     args = ap.parse_args()

@@ -190,6 +190,19 @@ int tsg_grid(tsg_handle* h, int32_t* out, void* stream);
  * query it; returns TSG_E_CAPACITY when cap is too small. */
 int tsg_neighbors(tsg_handle* h, int32_t* counts, int32_t* list, int64_t cap, int64_t* total, void* stream);
 
+/* Shape matching of every dynamic rigid body: centre of mass, A = sum m_V rho (x - cm)
+ * (x0 - rest cm)^T, its orthogonal polar factor R, x = cm + R (x0 - rest cm).  Replaces
+ * solve_rigid_body / solve_constraints (eng/solver_sph_base.py:472-500); tsg_step calls it
+ * after advect_something as SPHBase.step does.  The reference's ti.polar_decompose is
+ * replaced by Higham's scaled Newton iteration (orthogonal polar factor, converged to 1e-14).
+ * The reaction of the flow on dynamic rigid particles, which the reference scatters without
+ * synchronisation (eng/solver_sph_wc.py:70-71), is gathered by each rigid particle in
+ * ascending neighbour order inside tsg_one_step.  Dynamic rigid bodies take both forms for
+ * WCSPH and the FP64 form for the granular solvers (tsg_upload returns TSG_E_UNSUPPORTED
+ * for them in a granular FP32-mixed scene or a batched ensemble); a handle without dynamic
+ * rigid bodies returns 0 at once. */
+int tsg_solve_rigid_body(tsg_handle* h, void* stream);
+
 /* Density summation: out[i] = sum over the neighbours j != i of particle i (support radius,
  * the reference's traversal) of mass_j W(x_i - x_j), for every particle, in the current
  * particle order (the order of tsg_field views).  out is a device array of n doubles.

@@ -73,6 +73,7 @@ SYMBOLS = {
     "tsg_substep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "tsg_rk_update": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
     "tsg_density_sum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "tsg_solve_rigid_body": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "tsg_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "tsg_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(tsg_view), ctypes.c_void_p]),
     "tsg_particle_num": (ctypes.c_int64, [ctypes.c_void_p]),

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -61,6 +62,7 @@ struct tsg_handle {
     Fp32State* f32 = nullptr;       // FP32-mixed form (nullptr for FP64)
     int nscenes = 0;                // batched ensemble (tsg_batch_create): scenes and x pitch
     double batch_pitch = 0.0;
+    Rigid64 rigid{};                // dynamic rigid bodies (FP64 form)
 };
 
 namespace {
@@ -303,14 +305,40 @@ int upload_impl(tsg_handle* h, const tsg_particles* p, int from_device, void* st
         std::memcpy(mt.data(), p->mat_type, sizeof(int32_t) * h->n);
         std::memcpy(dyn.data(), p->is_dynamic, sizeof(int32_t) * h->n);
     }
-    int nflow = 0, nbdy = 0, nfluid = 0, nsoil = 0;
+    int nflow = 0, nbdy = 0, nfluid = 0, nsoil = 0, nrdyn = 0;
+    std::vector<int32_t> oid(h->n);
+    if (from_device) cudaMemcpy(oid.data(), p->obj_id, sizeof(int32_t) * h->n, cudaMemcpyDeviceToHost);
+    else std::memcpy(oid.data(), p->obj_id, sizeof(int32_t) * h->n);
+    std::vector<int> robj;          // dynamic rigid object ids and their particle counts
+    std::vector<int> rcount;
     for (int i = 0; i < h->n; ++i) {
         const int t = mt[i];
         if (t == MAT_FLUID) ++nfluid;
         else if (t == MAT_SOIL) ++nsoil;
         else if (t == MAT_DUMMY || t == MAT_REP) ++nbdy;
-        else if (t == MAT_RIGID) { if (dyn[i]) return TSG_E_UNSUPPORTED; ++nbdy; }
+        else if (t == MAT_RIGID) {
+            ++nbdy;
+            if (dyn[i]) {
+                ++nrdyn;
+                size_t q = 0;
+                while (q < robj.size() && robj[q] != oid[i]) ++q;
+                if (q == robj.size()) { robj.push_back(oid[i]); rcount.push_back(0); }
+                ++rcount[q];
+            }
+        }
         else return TSG_E_ARG;
+    }
+    // dynamic rigid bodies: both forms for WCSPH, the FP64 form for the granular solvers; not
+    // in batched ensembles
+    if (nrdyn && (scenes || (h->cfg.precision == TSG_FP32_MIXED && c.solver != 1))) return TSG_E_UNSUPPORTED;
+    c.n_rigid_dyn = nrdyn;
+    RigidObjects robjs;  // ids ascending, slices of the per-object particle lists
+    if (nrdyn) {
+        std::vector<size_t> order(robj.size());
+        for (size_t q = 0; q < order.size(); ++q) order[q] = q;
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return robj[a] < robj[b]; });
+        robjs.off.push_back(0);
+        for (size_t q : order) { robjs.ids.push_back(robj[q]); robjs.off.push_back(robjs.off.back() + rcount[q]); }
     }
     if ((c.solver == 1 && nsoil) || (c.solver != 1 && nfluid)) return TSG_E_UNSUPPORTED;
     nflow = c.solver == 1 ? nfluid : nsoil;
@@ -325,7 +353,7 @@ int upload_impl(tsg_handle* h, const tsg_particles* p, int from_device, void* st
             if (xz[3 * i + 2] != 0.0 || vz[3 * i + 2] != 0.0) return TSG_E_UNSUPPORTED;
     }
     if (h->cfg.precision == TSG_FP32_MIXED) {
-        int rc = fp32_create(h->cfg, c, p, from_device != 0, &h->f32, s, scenes);
+        int rc = fp32_create(h->cfg, c, p, from_device != 0, &h->f32, s, scenes, nrdyn ? &robjs : nullptr);
         if (rc) return rc;
         h->uploaded = true;
         return check_cuda();
@@ -343,10 +371,20 @@ int upload_impl(tsg_handle* h, const tsg_particles* p, int from_device, void* st
     if (c.solver != 1) upload_planes(h, p->stress, h->cur.stress, 9, dev, s);
     upload_ints(p->mat_type, h->cur.mat_type, h->n, dev, s);
     upload_ints(p->mat_id, h->cur.mat_id, h->n, dev, s);
+    if (nrdyn) {  // object table (ids ascending), list slices, rest centres of mass
+        Rigid64& rb = h->rigid;
+        rb.nobj = (int)robjs.ids.size();
+        if ((rc = dalloc(h, &rb.obj_id, robjs.ids.size())) || (rc = dalloc(h, &rb.off, robjs.off.size())) ||
+            (rc = dalloc(h, &rb.rest_cm, 3 * robjs.ids.size())) || (rc = dalloc(h, &rb.list, (size_t)nrdyn)))
+            return rc;
+        cudaMemcpy(rb.obj_id, robjs.ids.data(), sizeof(int) * robjs.ids.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(rb.off, robjs.off.data(), sizeof(int) * robjs.off.size(), cudaMemcpyHostToDevice);
+    }
     upload_ints(p->obj_id, h->cur.obj_id, h->n, dev, s);
     upload_ints(p->is_dynamic, h->cur.is_dynamic, h->n, dev, s);
     TSG_LAUNCH(k_iota, nb256(h->n), 256, s, h->cur.id0, h->n);
     if (c.solver == 3 && h->cfg.init_geostatic) fp64_init_geostatic(c, h->cur, h->d_scratch, s);
+    if (nrdyn) fp64_rest_cm(c, h->cur, h->rigid, s);
     h->uploaded = true;
     h->pos32_dirty = true;
     return check_cuda();
@@ -471,7 +509,9 @@ int tsg_step(tsg_handle* h, int nsteps, void* stream) {
         if ((rc = tsg_substep(h, stream))) return rc;
         if ((rc = tsg_advect(h, TSG_ADVECT_POS, stream))) return rc;
         if ((rc = tsg_advect(h, TSG_ADVECT_SOMETHING, stream))) return rc;
-        if (collide && (rc = tsg_advect(h, TSG_ENFORCE_BOUNDARY, stream))) return rc;
+        if (h->c.n_rigid_dyn && (rc = tsg_solve_rigid_body(h, stream))) return rc;
+        // enforce_boundary also clamps dynamic rigid particles in every boundary mode
+        if ((collide || h->c.n_rigid_dyn) && (rc = tsg_advect(h, TSG_ENFORCE_BOUNDARY, stream))) return rc;
     }
     return 0;
 }
@@ -672,6 +712,18 @@ int tsg_neighbors(tsg_handle* h, int32_t* counts, int32_t* list, int64_t cap, in
     cudaFree(tiles);
     int e = check_cuda();
     return rc ? rc : e;
+}
+
+int tsg_solve_rigid_body(tsg_handle* h, void* stream) {
+    if (!h || !h->uploaded) return TSG_E_STATE;
+    if (!h->c.n_rigid_dyn) return 0;  // no dynamic rigid body: nothing to solve
+    if (use_fp32(h)) {
+        fp32_solve_rigid(*h->f32, S(stream));
+    } else {
+        fp64_solve_rigid(h->c, h->cur, h->rigid, S(stream));
+        h->pos32_dirty = true;
+    }
+    return check_cuda();
 }
 
 int tsg_density_sum(tsg_handle* h, double* out, void* stream) {

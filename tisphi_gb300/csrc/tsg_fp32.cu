@@ -33,6 +33,7 @@
 // Reference: eng/particle_system.py:228-269 (cell list), eng/solver_sph_base.py:41-238,
 // :363-423, :648-669 (step, CSPM, boundary), eng/solver_sph_wc.py:82-132 (WCSPH).
 #include "tsg_fp32_dev.cuh"
+#include "tsg_polar.cuh"
 
 namespace tsg {
 
@@ -519,9 +520,162 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
             t.pr[i] = make_float2(pv, k.rho0);
             t.drt[i] = 0.f;
             p.vel[i].w = pv;
-            if (ti == MAT_RIGID) { t.dd[i] = 0.f; t.dv[i] = make_float4(0.f, 0.f, 0.f, 0.f); }
+            if (ti == MAT_RIGID) {  // static: rates stay zero; dynamic: gravity, then the reaction
+                t.dd[i] = 0.f;
+                t.dv[i] = tf_dyn(p.hi[i].w) ? make_float4(k.g[0], k.g[1], k.g[2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
         }
     });
+}
+
+// The reaction of the fluid on dynamic rigid particles (eng/solver_sph_wc.py:70-71, where
+// every fluid particle subtracts its pair term from its dynamic rigid neighbours without
+// synchronisation): each rigid particle gathers, over its list, the momentum pair term its
+// fluid neighbours' rates pass evaluates for it (viscosity in the boundary form with the
+// fluid particle's rho0 / rho~ factor, plus pressure, on the uncorrected gradient), and
+// subtracts it from the gravity its boundary pass set.  Compensated sums.
+template <int DIM>
+__global__ void k_rigid_reaction32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
+                                   const int* __restrict__ sstart) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.nd || t.cnt[i] > k.maxn) return;
+    const float wi = p.hi[i].w;
+    if (!(tf_type(wi) == MAT_RIGID && tf_dyn(wi))) return;
+    const float4 vti = t.vt[i];
+    const float mVi = p.lo[i].w;
+    CSum acc[3];
+    int m = 0;
+    for_nbrs_g<DIM, false, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
+                                 [&](int j) { return __ldg(t.vt + j); },
+                                 [&](int j, const float* dij, float r2, int, int cj, float, const float4& vtj) {
+        if (cj != kCodeFluid) return;
+        const float d[3] = {-dij[0], -dij[1], -dij[2]};  // x_fluid - x_rigid
+        const WG wg = w_pair<false, true>(k, r2);
+        const float mg = __fmul_rn(wg.g, mVi);
+        const float dvx = vtj.x - vti.x, dvy = vtj.y - vti.y, dvz = DIM == 3 ? vtj.z - vti.z : 0.f;
+        const float vdx = dvx * d[0] + dvy * d[1] + (DIM == 3 ? dvz * d[2] : 0.f);
+        const float rtj = k.rho0 + t.drt[j];
+        const float vf_b = k.visc_fac * (k.rho0 / rtj);
+        const float cv = vf_b * __fdividef(fminf(vdx, 0.f), r2 + k.eps_h2);
+        const float sc = mg * (cv + fmaf(-k.rho0, vti.w, -k.rho0 * vtj.w));
+        acc[0].add(-sc * d[0]);
+        acc[1].add(-sc * d[1]);
+        if (DIM == 3) acc[2].add(-sc * d[2]);
+        if (++m % kFlushEvery == 0) { acc[0].flush(); acc[1].flush(); acc[2].flush(); }
+    });
+    float4 dv = t.dv[i];
+    dv.x += acc[0].get();
+    dv.y += acc[1].get();
+    if (DIM == 3) dv.z += acc[2].get();
+    t.dv[i] = dv;
+}
+
+// Shape matching of one dynamic rigid object per block (eng/solver_sph_base.py:478-511):
+// the object's particles listed in ascending order, then in f64 by one thread the centre of
+// mass, A = sum (m_V rho p) q^T with p = x - cm and q = x0 - rest cm (q kept per id0), its
+// orthogonal polar factor R (identity when every entry is below 1e-8), and every particle
+// moved to cm + R q (its lo record takes the change; hi, a multiple of the list quantum,
+// stays until the next list build).
+__global__ void __launch_bounds__(1024) k_shape_match32(K32 k, P32 p, const int* __restrict__ ids_tab,
+                                                       const int* __restrict__ off, int* __restrict__ lists,
+                                                       const double* __restrict__ qtab) {
+    const int o = blockIdx.x;
+    const int oid = ids_tab[o];
+    int* list = lists + off[o];
+    __shared__ int warp_tot[32];
+    __shared__ int base_s;
+    __shared__ double cm_s[3], R_s[9];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) base_s = 0;
+    __syncthreads();
+    for (int i0 = 0; i0 < k.nd; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        bool on = false;
+        if (i < k.nd) {
+            const float w = p.hi[i].w;
+            on = tf_type(w) == MAT_RIGID && tf_dyn(w) && p.ids[i].z == oid;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, on);
+        if (lane == 0) warp_tot[wid] = __popc(bal);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int w = 0; w < nw; ++w) {
+            if (w < wid) before += warp_tot[w];
+            total += warp_tot[w];
+        }
+        if (on) list[base_s + before + __popc(bal & ((1u << lane) - 1u))] = i;
+        __syncthreads();
+        if (threadIdx.x == 0) base_s += total;
+        __syncthreads();
+    }
+    const int m = base_s;
+    if (threadIdx.x == 0) {
+        double cm[3] = {0.0, 0.0, 0.0}, sum_m = 0.0;
+        for (int q = 0; q < m; ++q) {
+            const int i = list[q];
+            const float4 h = p.hi[i], l = p.lo[i];
+            const double mi = p.mass[i];
+            cm[0] += mi * (k.vs[0] + ((double)h.x + (double)l.x));
+            cm[1] += mi * (k.vs[1] + ((double)h.y + (double)l.y));
+            cm[2] += mi * (k.vs[2] + ((double)h.z + (double)l.z));
+            sum_m += mi;
+        }
+        for (int d = 0; d < 3; ++d) cm[d] /= sum_m;
+        double A[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int q = 0; q < m; ++q) {
+            const int i = list[q];
+            const float4 h = p.hi[i], l = p.lo[i];
+            const double sc = (double)l.w * ((double)k.rho0 + (double)p.drho[i]);
+            const double* qq = qtab + 3 * (size_t)p.ids[i].x;
+            const double sp[3] = {sc * ((k.vs[0] + ((double)h.x + (double)l.x)) - cm[0]),
+                                  sc * ((k.vs[1] + ((double)h.y + (double)l.y)) - cm[1]),
+                                  sc * ((k.vs[2] + ((double)h.z + (double)l.z)) - cm[2])};
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) A[3 * a + b] += sp[a] * qq[b];
+        }
+        double R[9];
+        polar3(A, R);
+        bool small = true;
+        for (int q = 0; q < 9; ++q) small = small && fabs(R[q]) < EPS;
+        if (small)
+            for (int q = 0; q < 9; ++q) R[q] = (q % 4 == 0) ? 1.0 : 0.0;
+        for (int d = 0; d < 3; ++d) cm_s[d] = cm[d];
+        for (int q = 0; q < 9; ++q) R_s[q] = R[q];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+        const int i = list[q];
+        const double* qq = qtab + 3 * (size_t)p.ids[i].x;
+        const float4 h = p.hi[i];
+        float4 l = p.lo[i];
+        const double g0 = cm_s[0] + ((R_s[0] * qq[0] + R_s[1] * qq[1]) + R_s[2] * qq[2]);
+        const double g1 = cm_s[1] + ((R_s[3] * qq[0] + R_s[4] * qq[1]) + R_s[5] * qq[2]);
+        const double g2 = cm_s[2] + ((R_s[6] * qq[0] + R_s[7] * qq[1]) + R_s[8] * qq[2]);
+        l.x = (float)((g0 - k.vs[0]) - (double)h.x);
+        l.y = (float)((g1 - k.vs[1]) - (double)h.y);
+        if (k.dim == 3) l.z = (float)((g2 - k.vs[2]) - (double)h.z);
+        p.lo[i] = l;
+    }
+}
+
+// init_rigid_body (eng/solver_sph_base.py:467-470) from the uploaded f64 positions in upload
+// order: one thread per object sums its rest centre of mass, then every dynamic rigid
+// particle's rest offset x0 - rest cm is stored at its upload index (its id0).
+__global__ void k_rigid_rest32(int n, const int* __restrict__ ids_tab, const double* __restrict__ x,
+                               const double* __restrict__ mass, const int* __restrict__ mt,
+                               const int* __restrict__ oid, const int* __restrict__ dyn, double* __restrict__ q) {
+    if (threadIdx.x != 0) return;
+    const int o = blockIdx.x;
+    double cm[3] = {0.0, 0.0, 0.0}, sum_m = 0.0;
+    for (int i = 0; i < n; ++i) {
+        if (!(mt[i] == MAT_RIGID && dyn[i] && oid[i] == ids_tab[o])) continue;
+        for (int d = 0; d < 3; ++d) cm[d] += mass[i] * x[3 * (size_t)i + d];
+        sum_m += mass[i];
+    }
+    for (int d = 0; d < 3; ++d) cm[d] /= sum_m;
+    for (int i = 0; i < n; ++i)
+        if (mt[i] == MAT_RIGID && dyn[i] && oid[i] == ids_tab[o])
+            for (int d = 0; d < 3; ++d) q[3 * (size_t)i + d] = x[3 * (size_t)i + d] - cm[d];
 }
 
 // WCSPH continuity + momentum (eng/solver_sph_wc.py:108-126).
@@ -1612,7 +1766,7 @@ __global__ void k_offset(int* a, long long m, int off) {
 }  // namespace
 
 int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp, bool from_device,
-                Fp32State** out, cudaStream_t s, const Fp32Scenes* scenes) {
+                Fp32State** out, cudaStream_t s, const Fp32Scenes* scenes, const RigidObjects* rigid) {
     *out = nullptr;
     if (c.n > (1 << kEntryBits)) return TSG_E_CAPACITY;  // neighbour-list entries index 2^23 particles
 
@@ -1760,6 +1914,17 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
         cudaStreamSynchronize(s);
         k.scene_par = dpar;
         st->nscenes = scenes->nscenes;
+    }
+    if (rigid && !rigid->ids.empty()) {  // dynamic rigid bodies: object table and rest offsets
+        st->rnobj = (int)rigid->ids.size();
+        st->r_ids = dal<int>(*st, rigid->ids.size());
+        st->r_off = dal<int>(*st, rigid->off.size());
+        st->r_list = dal<int>(*st, (size_t)rigid->off.back() + 1);
+        st->r_q = dal<double>(*st, 3 * (size_t)n);
+        if (!st->r_q) { fp32_destroy(st); return TSG_E_CUDA; }
+        cudaMemcpyAsync(st->r_ids, rigid->ids.data(), sizeof(int) * rigid->ids.size(), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(st->r_off, rigid->off.data(), sizeof(int) * rigid->off.size(), cudaMemcpyHostToDevice, s);
+        TSG_LAUNCH(k_rigid_rest32, st->rnobj, 32, s, n, st->r_ids, dx, d2, imt, ioid, idyn, st->r_q);
     }
     TSG_LAUNCH(k_load32, nblk(n), TPB, s, k, dx, dv, d1, d2, d3, d4, imt, imid, ioid, idyn, islot, iscene, st->P[0]);
     if (soil && pp->stress) {  // (n, 3, 3) row-major -> six planes (upper triangle)
@@ -2151,6 +2316,10 @@ static void one_step(Fp32State& st, cudaStream_t s, bool eos, bool fl = false, b
             else { if (k.corr) rates_launch<3, true, true>(st, p, s, ovf); else rates_launch<3, false, true>(st, p, s, ovf); }
         } else if (k.dim == 2) { if (k.corr) rates_launch<2, true>(st, p, s, ovf); else rates_launch<2, false>(st, p, s, ovf); }
         else { if (k.corr) rates_launch<3, true>(st, p, s, ovf); else rates_launch<3, false>(st, p, s, ovf); }
+        if (st.rnobj) {  // the fluid's reaction on dynamic rigid particles, after the rates pass
+            if (k.dim == 2) TSG_LAUNCH(k_rigid_reaction32<2>, nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart);
+            else TSG_LAUNCH(k_rigid_reaction32<3>, nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart);
+        }
     }
 }
 
@@ -2257,7 +2426,8 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide, bool fold_disp)
             TSG_LAUNCH(k_advect_final_wc32, nblk(st.k.nd), TPB, s, st.k, st.P[st.cur], st.T, st.err, st.pf,
                        fold_disp ? st.maxdisp : nullptr);
             if (st.k.disp2_limit <= 0.f) st.lists_valid = false;
-            if (collide) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
+            fp32_solve_rigid(st, s);
+            if (collide || st.rnobj) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
             return;
         }
         fp32_advect(st, TSG_ADVECT_FULL, s);
@@ -2268,7 +2438,14 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide, bool fold_disp)
         advect_pos(st, s, false);
         fp32_advect(st, TSG_ADVECT_SOMETHING, s);
     }
-    if (collide) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
+    fp32_solve_rigid(st, s);
+    if (collide || st.rnobj) fp32_advect(st, TSG_ENFORCE_BOUNDARY, s);
+}
+
+void fp32_solve_rigid(Fp32State& st, cudaStream_t s) {
+    if (st.rnobj == 0) return;
+    PhaseScope ph(s, PH_POS);
+    TSG_LAUNCH(k_shape_match32, st.rnobj, 1024, s, st.k, st.P[st.cur], st.r_ids, st.r_off, st.r_list, st.r_q);
 }
 
 void fp32_step_body(Fp32State& st, bool collide, cudaStream_t s) { f32::step_body(st, s, collide); }
@@ -2292,7 +2469,8 @@ void fold_rebuilds(Fp32State& st, cudaStream_t s) {
 // Whether step_body ends with the fused final update (which folds the new positions into
 // the displacement maximum) and moves no particle after it.
 bool folds_disp(const Fp32State& st, bool collide) {
-    return st.k.solver == 1 && st.c.ti != 4 && !st.k.xsph && !collide && st.k.disp2_limit > 0.f;
+    // (shape matching and the boundary clamp move particles after the fused update)
+    return st.k.solver == 1 && st.c.ti != 4 && !st.k.xsph && !collide && st.rnobj == 0 && st.k.disp2_limit > 0.f;
 }
 
 // IF node whose body re-sorts in place and rebuilds the lists, then the step body.

@@ -1,5 +1,6 @@
 // FP32-mixed form: interface used by the C ABI layer (tsg_api.cu).
 #pragma once
+#include <vector>
 #include "tsg_internal.h"
 
 namespace tsg {
@@ -15,8 +16,15 @@ struct Fp32Scenes {
     int nscenes = 0;
 };
 
+// Dynamic rigid objects of a scene: ids ascending, off[o] .. off[o + 1] their slice of a
+// list of n_rigid_dyn particles.
+struct RigidObjects {
+    std::vector<int> ids, off;
+};
 int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* p, bool from_device,
-                Fp32State** out, cudaStream_t s, const Fp32Scenes* scenes = nullptr);
+                Fp32State** out, cudaStream_t s, const Fp32Scenes* scenes = nullptr,
+                const RigidObjects* rigid = nullptr);
+void fp32_solve_rigid(Fp32State& st, cudaStream_t s);
 void fp32_destroy(Fp32State* st);
 void fp32_sort(Fp32State& st, cudaStream_t s);
 // True when the neighbour lists must be rebuilt before the next step (always without a skin).

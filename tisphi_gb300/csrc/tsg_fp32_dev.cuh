@@ -532,6 +532,11 @@ struct Fp32State {
     int *cells_d = nullptr, *cells_s = nullptr, *ncells = nullptr;  // non-empty cells (dynamic, static)
     int *ovf_list = nullptr, *novf = nullptr;  // particles whose neighbours exceed the list capacity
     int *sact = nullptr, *nsact = nullptr;     // static-block particles with a non-empty list
+    // dynamic rigid bodies (WCSPH): objects, per-object list slices, and each rigid
+    // particle's rest offset x0 - rest centre of mass in f64, indexed by id0
+    int rnobj = 0;
+    int *r_ids = nullptr, *r_off = nullptr, *r_list = nullptr;
+    double* r_q = nullptr;
     unsigned* maxdisp = nullptr;               // squared displacement since the last list build
     bool built = false;
     double* stage = nullptr;       // f64 export staging (9 n)

@@ -25,6 +25,7 @@
 #include <cfloat>
 
 #include "tsg_internal.h"
+#include "tsg_polar.cuh"
 
 namespace tsg {
 
@@ -356,9 +357,10 @@ __global__ void k_bdy(Consts c, Persist64 p, Trans64 t, const int* __restrict__ 
         t.density_tmp[i] = c.solver == 2 ? fmax(bd * f, c.rho0) : c.rho0;
         for (int q = 0; q < 9; ++q) t.stress_tmp[(size_t)q * n + i] = bs[q] * f;
     }
-    if (ti == MAT_RIGID) {  // static rigid: rates stay zero (dynamic rigid is rejected at create)
+    if (ti == MAT_RIGID) {  // static rigid: rates stay zero; dynamic rigid: gravity, then the reaction
         t.d_density[i] = 0.0;
-        for (int d = 0; d < 3; ++d) t.d_vel[(size_t)d * n + i] = 0.0;
+        const bool dyn = p.is_dynamic[i] != 0;
+        for (int d = 0; d < 3; ++d) t.d_vel[(size_t)d * n + i] = dyn ? c.g[d] : 0.0;
     }
 }
 
@@ -373,6 +375,28 @@ __device__ __forceinline__ void rep_force(const Consts& c, const double* r, doub
     else if (gm > 1 && gm < 2) f = 0.5 * ((2 - gm) * (2 - gm));
     double s = c.rep_fac * chi * f / (rn * rn);
     for (int d = 0; d < DIM; ++d) acc[d] = acc[d] + s * r[d];
+}
+
+// One neighbour's term of calc_d_vel_task (eng/solver_sph_wc.py:34-71): viscosity
+// (fluid, or boundary / rigid neighbours with the rho0 / rho~_i factor) plus pressure, for
+// centre i and neighbour j of type tj; dvv = v~_i - v~_j, r = x_i - x_j, kd = grad W(r).
+template <int DIM>
+__device__ __forceinline__ void wc_force_pair(const Consts& c, int tj, double mVj, const double* dvv, double rti,
+                                              double pri, double ptj, double rtj, const double* r, double rn,
+                                              const double* kd, double* out) {
+    const double mn = fmin(dotv<DIM>(dvv, r), 0.0);
+    const double den = rn * rn + c.eps_h2;
+    double cv = 0.0;
+    bool visc = false;
+    if (tj == MAT_FLUID) { cv = c.visc_fac * mVj * mn / den; visc = true; }
+    else if (tj == MAT_DUMMY || tj == MAT_REP || tj == MAT_RIGID) {
+        cv = c.visc_fac * mVj * c.rho0 / rti * mn / den; visc = true;
+    }
+    const double cp = -c.rho0 * mVj * (pri + ptj / (rtj * rtj));
+    for (int d = 0; d < DIM; ++d) {
+        double pv = cp * kd[d];
+        out[d] = visc ? cv * kd[d] + pv : 0.0 + pv;
+    }
 }
 
 // ---- WCSPH rates (eng/solver_sph_wc.py:108-126) ----
@@ -412,22 +436,9 @@ __global__ void k_wc_rates(Consts c, Persist64 p, Trans64 t, const int* __restri
         } else {
             dd += dotv<DIM>(a, kd);
         }
-        // viscosity (eng/solver_sph_wc.py:34-46)
-        const double mn = fmin(dotv<DIM>(dvv, r), 0.0);
-        const double den = rn * rn + c.eps_h2;
-        double cv = 0.0;
-        bool visc = false;
-        if (tj == MAT_FLUID) { cv = c.visc_fac * mVj * mn / den; visc = true; }
-        else if (tj == MAT_DUMMY || tj == MAT_REP || tj == MAT_RIGID) {
-            cv = c.visc_fac * mVj * c.rho0 / rti * mn / den; visc = true;
-        }
-        // pressure (eng/solver_sph_wc.py:49-55)
-        const double rtj = t.density_tmp[j];
-        const double cp = -c.rho0 * mVj * (pri + p.pressure[j] / (rtj * rtj));
-        for (int d = 0; d < DIM; ++d) {
-            double pv = cp * kd[d];
-            dv[d] += visc ? cv * kd[d] + pv : 0.0 + pv;
-        }
+        double f[3];
+        wc_force_pair<DIM>(c, tj, mVj, dvv, rti, pri, p.pressure[j], t.density_tmp[j], r, rn, kd, f);
+        for (int d = 0; d < DIM; ++d) dv[d] += f[d];
     });
     if (rep) {  // separate traversal: the reference adds these after the whole dv sum
         for_neighbors<DIM>(c, p.x, t.pos32, cs, i, xi, true, [&](int j, const double* r, double rn) {
@@ -497,8 +508,8 @@ __global__ void k_mui_stress(Consts c, Persist64 p, Trans64 t, const int* __rest
 
 // Stress-divergence sum (eng/solver_sph_muI.py:39-46), shared by mu(I) and DP.
 template <int DIM>
-__device__ __forceinline__ void stress_div_term(const double* sti, double ri2, const double* stj, double rtj,
-                                                double mVj, const double* kc, double* acc) {
+__device__ __forceinline__ void stress_div_val(const double* sti, double ri2, const double* stj, double rtj,
+                                               double mVj, const double* kc, double* out) {
     const double rj2 = rtj * rtj;
     const double sc = mVj * rtj;
     for (int a = 0; a < DIM; ++a) {
@@ -508,8 +519,15 @@ __device__ __forceinline__ void stress_div_term(const double* sti, double ri2, c
             double v = (sc * m) * kc[b];
             s = b == 0 ? v : s + v;
         }
-        acc[a] += s;
+        out[a] = s;
     }
+}
+template <int DIM>
+__device__ __forceinline__ void stress_div_term(const double* sti, double ri2, const double* stj, double rtj,
+                                                double mVj, const double* kc, double* acc) {
+    double v[3];
+    stress_div_val<DIM>(sti, ri2, stj, rtj, mVj, kc, v);
+    for (int a = 0; a < DIM; ++a) acc[a] += v[a];
 }
 
 template <int DIM>
@@ -960,6 +978,157 @@ __global__ void k_ymax_soil(Consts c, Persist64 p, double* out) {
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
+// ---- dynamic rigid bodies (eng/solver_sph_base.py:467-518) ----
+// The reaction on dynamic rigid particles.  The reference subtracts every flow particle's
+// pair term from its dynamic rigid neighbour inside the flow particle's loop
+// (`pt[j].d_vel -= tmp`, eng/solver_sph_wc.py:70-71, eng/solver_sph_muI.py:45-46,
+// eng/solver_sph_dp.py:164-165), an unsynchronised scatter.  Here every rigid particle
+// gathers the terms of its flow neighbours in its own traversal order, which is ascending
+// particle index (the serial order of the scatter), evaluating each term exactly as the flow
+// particle's loop does (r = x_flow - x_rigid is the exact negation of the traversal's
+// offset), starting from the gravity the boundary pass set.
+template <int DIM>
+__global__ void k_rigid_reaction(Consts c, Persist64 p, Trans64 t, const int* __restrict__ cs,
+                                 const int* __restrict__ list, int count) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int j = list[k];
+    if (!(p.mat_type[j] == MAT_RIGID && p.is_dynamic[j])) return;
+    const int n = c.n;
+    double xj[3];
+    load_x<DIM>(p.x, j, n, xj);
+    double dvj[3];
+    for (int d = 0; d < 3; ++d) dvj[d] = t.d_vel[(size_t)d * n + j];
+    const double mVj = p.m_V[j], rtj = t.density_tmp[j], ptj = p.pressure[j];
+    double stj[9], vtj[3];
+    if (c.solver != 1)
+        for (int q = 0; q < 9; ++q) stj[q] = t.stress_tmp[(size_t)q * n + j];
+    for (int d = 0; d < 3; ++d) vtj[d] = t.v_tmp[(size_t)d * n + j];
+    for_neighbors<DIM>(c, p.x, t.pos32, cs, j, xj, true, [&](int i, const double* rji, double rn) {
+        if (p.mat_type[i] != c.flow_type) return;
+        double r[3] = {-rji[0], -rji[1], -rji[2]};
+        if (DIM == 2) r[2] = 0.0;
+        double kd[3], f[3] = {0.0, 0.0, 0.0};
+        kernel_dW<DIM>(c, r, rn, kd);
+        const double rti = t.density_tmp[i];
+        if (c.solver == 1) {
+            double dvv[3];
+            for (int d = 0; d < DIM; ++d) dvv[d] = t.v_tmp[(size_t)d * n + i] - vtj[d];
+            const double pri = p.pressure[i] / (rti * rti);
+            wc_force_pair<DIM>(c, MAT_RIGID, mVj, dvv, rti, pri, ptj, rtj, r, rn, kd, f);
+        } else {
+            double kc[3], sti[9];
+            if (c.corr == 1) {
+                double L[9];
+                for (int q = 0; q < 9; ++q) L[q] = t.CSPM_L[(size_t)q * n + i];
+                matvec_corr<DIM>(L, kd, kc);
+            } else {
+                kc[0] = kd[0]; kc[1] = kd[1]; kc[2] = kd[2];
+            }
+            for (int q = 0; q < 9; ++q) sti[q] = t.stress_tmp[(size_t)q * n + i];
+            stress_div_val<DIM>(sti, rti * rti, stj, rtj, mVj, kc, f);
+        }
+        for (int d = 0; d < DIM; ++d) dvj[d] = dvj[d] - f[d];
+    });
+    for (int d = 0; d < 3; ++d) t.d_vel[(size_t)d * n + j] = dvj[d];
+}
+
+// init_rigid_body / calc_rigid_rest_m (eng/solver_sph_base.py:467-470, :517-518): the rest
+// centre of mass of every dynamic rigid object from the uploaded positions, summed in upload
+// order by one thread per object (before the first sort).
+__global__ void k_rest_cm(Consts c, Persist64 p, Rigid64 rb) {
+    const int o = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    const int oid = rb.obj_id[o];
+    const int n = c.n;
+    double cm[3] = {0.0, 0.0, 0.0}, sum_m = 0.0;
+    for (int i = 0; i < n; ++i) {
+        if (!(p.mat_type[i] == MAT_RIGID && p.is_dynamic[i] && p.obj_id[i] == oid)) continue;
+        const double mi = p.mass[i];
+        for (int d = 0; d < 3; ++d) cm[d] = cm[d] + mi * p.x[(size_t)d * n + i];
+        sum_m += mi;
+    }
+    for (int d = 0; d < 3; ++d) rb.rest_cm[3 * o + d] = cm[d] / sum_m;
+}
+
+// solve_constraints (eng/solver_sph_base.py:478-500), one block per dynamic rigid object:
+// the object's particles listed in ascending order (block-wide ballot compaction), then by
+// one thread in that order the centre of mass (calc_cm, :502-511) and
+// A = sum (m_V rho p) q^T (p = x - cm, q = x0 - rest cm), R = polar(A) (identity when every
+// entry is below 1e-8), and finally every particle x += (cm + R q) - x.
+__global__ void __launch_bounds__(1024) k_shape_match(Consts c, Persist64 p, Rigid64 rb) {
+    const int o = blockIdx.x;
+    const int oid = rb.obj_id[o];
+    int* list = rb.list + rb.off[o];
+    __shared__ int warp_tot[32];
+    __shared__ int base_s;
+    __shared__ double cm_s[3], R_s[9];
+    const int n = c.n;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) base_s = 0;
+    __syncthreads();
+    for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const bool on = i < n && p.mat_type[i] == MAT_RIGID && p.is_dynamic[i] && p.obj_id[i] == oid;
+        const unsigned bal = __ballot_sync(0xffffffffu, on);
+        if (lane == 0) warp_tot[wid] = __popc(bal);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int w = 0; w < nw; ++w) {
+            if (w < wid) before += warp_tot[w];
+            total += warp_tot[w];
+        }
+        if (on) list[base_s + before + __popc(bal & ((1u << lane) - 1u))] = i;
+        __syncthreads();
+        if (threadIdx.x == 0) base_s += total;
+        __syncthreads();
+    }
+    const int m = base_s;
+    if (threadIdx.x == 0) {
+        double cm[3] = {0.0, 0.0, 0.0}, sum_m = 0.0;
+        for (int k = 0; k < m; ++k) {
+            const int i = list[k];
+            const double mi = p.mass[i];
+            for (int d = 0; d < 3; ++d) cm[d] = cm[d] + mi * p.x[(size_t)d * n + i];
+            sum_m += mi;
+        }
+        for (int d = 0; d < 3; ++d) cm[d] = cm[d] / sum_m;
+        double A[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < m; ++k) {
+            const int i = list[k];
+            const double sc = p.m_V[i] * p.density[i];
+            double sp[3], q[3];
+            for (int d = 0; d < 3; ++d) {
+                q[d] = p.x0[(size_t)d * n + i] - rb.rest_cm[3 * o + d];
+                sp[d] = sc * (p.x[(size_t)d * n + i] - cm[d]);
+            }
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) A[3 * a + b] = A[3 * a + b] + sp[a] * q[b];
+        }
+        double R[9];
+        polar3(A, R);
+        bool small = true;
+        for (int q = 0; q < 9; ++q) small = small && fabs(R[q]) < EPS;
+        if (small)
+            for (int q = 0; q < 9; ++q) R[q] = (q % 4 == 0) ? 1.0 : 0.0;
+        for (int d = 0; d < 3; ++d) cm_s[d] = cm[d];
+        for (int q = 0; q < 9; ++q) R_s[q] = R[q];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        const int i = list[k];
+        double q[3];
+        for (int d = 0; d < 3; ++d) q[d] = p.x0[(size_t)d * n + i] - rb.rest_cm[3 * o + d];
+        for (int a = 0; a < 3; ++a) {
+            const double rq = (R_s[3 * a] * q[0] + R_s[3 * a + 1] * q[1]) + R_s[3 * a + 2] * q[2];
+            const double goal = cm_s[a] + rq;
+            const double xa = p.x[(size_t)a * n + i];
+            const double corr = (goal - xa) * 1.0;
+            p.x[(size_t)a * n + i] = xa + corr;
+        }
+    }
+}
+
 #define DISPATCH_DIM(c, KERNEL, GRID, ...)                                   \
     do {                                                                     \
         if ((c).dim == 2) TSG_LAUNCH(KERNEL<2>, GRID, TPB, s, __VA_ARGS__);       \
@@ -969,6 +1138,16 @@ __global__ void k_ymax_soil(Consts c, Persist64 p, double* out) {
 void fp64_kernel_corr(const Consts& c, const Persist64& p, Trans64& t, const Grid& g, cudaStream_t s) {
     PhaseScope ph(s, PH_CORR);
     DISPATCH_DIM(c, k_corr, nblk(c.n), c, p, t, g.cell_start);
+}
+
+void fp64_rest_cm(const Consts& c, const Persist64& p, const Rigid64& r, cudaStream_t s) {
+    if (r.nobj > 0) TSG_LAUNCH(k_rest_cm, r.nobj, 32, s, c, p, r);
+}
+
+void fp64_solve_rigid(const Consts& c, Persist64& p, const Rigid64& r, cudaStream_t s) {
+    if (r.nobj <= 0) return;
+    PhaseScope ph(s, PH_POS);
+    TSG_LAUNCH(k_shape_match, r.nobj, 1024, s, c, p, r);
 }
 
 void fp64_density_sum(const Consts& c, const Persist64& p, const Trans64& t, const Grid& g, double* out,
@@ -1000,6 +1179,10 @@ void fp64_one_step(const Consts& c, Persist64& p, Trans64& t, const Grid& g, cud
         if (c.solver == 1) DISPATCH_DIM(c, k_wc_rates, nblk(c.n_flow), c, p, t, g.cell_start, g.list_flow, c.n_flow);
         else if (c.solver == 2) DISPATCH_DIM(c, k_mui_mom, nblk(c.n_flow), c, p, t, g.cell_start, g.list_flow, c.n_flow);
         else DISPATCH_DIM(c, k_dp_rates, nblk(c.n_flow), c, p, t, g.cell_start, g.list_flow, c.n_flow);
+    }
+    if (c.n_rigid_dyn > 0 && c.n_bdy > 0) {  // the flow's reaction on dynamic rigid particles
+        PhaseScope ph(s, PH_RATES);
+        DISPATCH_DIM(c, k_rigid_reaction, nblk(c.n_bdy), c, p, t, g.cell_start, g.list_bdy, c.n_bdy);
     }
 }
 

@@ -53,6 +53,18 @@ struct Consts {
     // every |x - vdomain_start| below pf_lim
     int pf_on;
     float pf_r2, pf_lim;
+    int n_rigid_dyn;    // dynamic rigid particles (shape-matched bodies)
+};
+
+// Dynamic rigid bodies (eng/solver_sph_base.py:467-518): object ids, rest centres of mass
+// (from the uploaded positions, in upload order) and, per object, the slice of `list`
+// that the shape-matching kernel fills with the object's particles in ascending order.
+struct Rigid64 {
+    int nobj = 0;
+    int* obj_id = nullptr;      // nobj (device)
+    double* rest_cm = nullptr;  // 3 nobj (device)
+    int* off = nullptr;         // nobj + 1 (device): slice starts in list
+    int* list = nullptr;        // n_rigid_dyn (device)
 };
 
 // Persistent per-particle fields (permuted by the sort; double-buffered).
@@ -134,6 +146,8 @@ void fp64_rk_update(const Consts& c, Persist64& p, Trans64& t, int m, cudaStream
 void fp64_neighbors(const Consts& c, const Persist64& p, const Trans64& t, const Grid& g,
                     int* counts, int* offsets, int* list, cudaStream_t s);
 void fp64_diag(const Consts& c, const Persist64& p, double* out8, cudaStream_t s);
+void fp64_solve_rigid(const Consts& c, Persist64& p, const Rigid64& r, cudaStream_t s);
+void fp64_rest_cm(const Consts& c, const Persist64& p, const Rigid64& r, cudaStream_t s);
 void fp64_density_sum(const Consts& c, const Persist64& p, const Trans64& t, const Grid& g, double* out,
                       cudaStream_t s);
 void fp64_init_geostatic(const Consts& c, Persist64& p, double* scratch, cudaStream_t s);

@@ -104,5 +104,6 @@ class SPHBase:
         self._call("tsg_advect", nat.TSG_ENFORCE_BOUNDARY)
 
     def solve_rigid_body(self):
-        """Dynamic rigid bodies are rejected at upload, so there is nothing to solve."""
-        return None
+        """Shape matching of the dynamic rigid bodies (eng/solver_sph_base.py:472-500); step()
+        calls it after advect_something."""
+        self._call("tsg_solve_rigid_body")
