@@ -436,7 +436,7 @@ __global__ void k_adj_out(K32 k, P32 p, Start S, A32 A, double* __restrict__ ax,
     }
 }
 
-__global__ void k_copy_start(int n, P32 p, const float4* __restrict__ vt, Start S) {
+__global__ void k_copy_start(int n, P32 p, RecView vt, Start S) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     S.hi[i] = p.hi[i];
@@ -750,7 +750,7 @@ int fp32_adjoint_step(Fp32State& st, double* ax, double* av, double* ar, double*
     AdjBuffers* B = adj_buffers(st);
     if (!B) return TSG_E_CUDA;
     // forward of the step from the loaded state, keeping its start
-    f32::rebuild(st, s, false);  // re-sorts into the other buffer and makes it current
+    f32::rebuild(st, s, true);  // in place: v_tmp lives in the current buffer's records
     st.built = true;
     st.lists_valid = true;
     ++st.rebuilds;

@@ -42,7 +42,7 @@ using namespace f32;
 namespace {
 
 // ---------------------------------------------------------------- sort (dynamic block)
-__global__ void k_hash32(K32 k, int count_n, int base, const float4* __restrict__ HI, const float4* __restrict__ LO,
+__global__ void k_hash32(K32 k, int count_n, int base, const float4* __restrict__ HI, RecView LO,
                          int* __restrict__ cell_of, int* __restrict__ rank, int* __restrict__ count, int* __restrict__ err) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count_n) return;
@@ -122,7 +122,7 @@ __device__ __forceinline__ void note_overflow(int* ovf_list, int* novf, int i) {
 
 // ---------------------------------------------------------------- neighbour lists
 template <int DIM>
-__global__ void k_lists(K32 k, const float4* __restrict__ HI, const float4* __restrict__ LO,
+__global__ void k_lists(K32 k, const float4* __restrict__ HI, RecView LO,
                         const float4* __restrict__ PF, const int* __restrict__ dstart, const int* __restrict__ sstart,
                         int* __restrict__ cnt, int* __restrict__ nbr, int* __restrict__ ovf_list, int* __restrict__ novf) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -145,7 +145,7 @@ __global__ void k_lists(K32 k, const float4* __restrict__ HI, const float4* __re
 // out-of-grid bin take the per-particle path.
 template <int DIM, int WPB>
 __global__ void k_lists_cell(K32 k, int self_blk, const int* __restrict__ cells, const int* __restrict__ cell_count,
-                             const float4* __restrict__ HI, const float4* __restrict__ LO,
+                             const float4* __restrict__ HI, RecView LO,
                              const float4* __restrict__ PF, const int* __restrict__ dstart,
                              const int* __restrict__ sstart, int* __restrict__ cnt, int* __restrict__ nbr,
                              int* __restrict__ ovf_list, int* __restrict__ novf) {
@@ -267,7 +267,7 @@ __global__ void k_nonempty_cells(long long G, const int* __restrict__ start, int
 // Per-particle list build for particles the warp-per-cell pass could not serve (their true
 // cell differs from the storage cell); flagged with count -1.
 template <int DIM>
-__global__ void k_lists_fixup(K32 k, const float4* __restrict__ HI, const float4* __restrict__ LO,
+__global__ void k_lists_fixup(K32 k, const float4* __restrict__ HI, RecView LO,
                               const float4* __restrict__ PF, const int* __restrict__ dstart,
                               const int* __restrict__ sstart, int* __restrict__ cnt, int* __restrict__ nbr,
                               int* __restrict__ ovf_list, int* __restrict__ novf) {
@@ -288,7 +288,7 @@ __global__ void k_lists_fixup(K32 k, const float4* __restrict__ HI, const float4
 // Per-particle list build for an index range (out-of-grid bin).
 template <int DIM>
 __global__ void k_lists_range(K32 k, const int* __restrict__ bounds, const float4* __restrict__ HI,
-                              const float4* __restrict__ LO, const float4* __restrict__ PF,
+                              RecView LO, const float4* __restrict__ PF,
                               const int* __restrict__ dstart, const int* __restrict__ sstart,
                               int* __restrict__ cnt, int* __restrict__ nbr, int* __restrict__ ovf_list,
                               int* __restrict__ novf) {
@@ -489,10 +489,12 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
         const int ti = tf_type(p.hi[i].w);
         if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
             CSum bv[3], bp, sh;
-            for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
-                              [&](int j, const float* d, float r2, int sidx, int, float mV) {
+            // the neighbour's v_tmp comes with its lo record (one 256-bit read)
+            for_nbrs_g<DIM, FB, false, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
+                                             [&](int j) { return t.vt[j]; },
+                                             [&](int j, const float* d, float r2, int sidx, int, float mV,
+                                                 const float4& vt) {
                 const float w = w_pair<true, false, KT>(k, r2).w;
-                const float4 vt = t.vt[j];
                 const float2 pr = t.pr[j];
                 const float mw = mV * w;
                 if (SH) sh.p = __fmaf_rn(mV, w, sh.p);
@@ -546,7 +548,7 @@ __global__ void k_rigid_reaction32(K32 k, P32 p, T32 t, const float4* __restrict
     CSum acc[3];
     int m = 0;
     for_nbrs_g<DIM, false, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
-                                 [&](int j) { return __ldg(t.vt + j); },
+                                 [&](int j) { return t.vt[j]; },
                                  [&](int j, const float* dij, float r2, int, int cj, float, const float4& vtj) {
         if (cj != kCodeFluid) return;
         const float d[3] = {-dij[0], -dij[1], -dij[2]};  // x_fluid - x_rigid
@@ -710,8 +712,8 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         // viscosity factor for fluid and for boundary neighbours; -rho0 p_i / rho_i^2
         const float vf_f = visc_fac, vf_b = visc_fac * visc_b;
         const float pi_n = -k.rho0 * vti.w;
-        for_nbrs_g<DIM, FB, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
-                                  [&](int j) { return __ldg(t.vt + j); },
+        for_nbrs_g<DIM, FB, true, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
+                                        [&](int j) { return t.vt[j]; },
                                   [&](int, const float* d, float r2, int sidx, int cj, float mVj, const float4& vtj) {
             const WG wg = w_pair<FL, true, KT>(k, r2);
             const float r = wg.r;
@@ -1563,7 +1565,7 @@ __global__ void k_load_stress32(K32 k, const double* __restrict__ st, const int*
 
 // Inspection: enumerate every neighbour directly (independent of the ELL capacity).
 template <int DIM>
-__global__ void k_nbr_count32(K32 k, const float4* HI, const float4* LO, const float4* PF, const int* ds,
+__global__ void k_nbr_count32(K32 k, const float4* HI, RecView LO, const float4* PF, const int* ds,
                               const int* ss, int* counts) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
@@ -1574,7 +1576,7 @@ __global__ void k_nbr_count32(K32 k, const float4* HI, const float4* LO, const f
 }
 
 template <int DIM>
-__global__ void k_nbr_fill32(K32 k, const float4* HI, const float4* LO, const float4* PF, const int* ds,
+__global__ void k_nbr_fill32(K32 k, const float4* HI, RecView LO, const float4* PF, const int* ds,
                              const int* ss, const int* off, int* list) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
@@ -1584,7 +1586,7 @@ __global__ void k_nbr_fill32(K32 k, const float4* HI, const float4* LO, const fl
 }
 
 template <int DIM>
-__global__ void k_nbr_count_ell(K32 k, const float4* HI, const float4* LO, const int* cnt, const int* nbr, int* counts) {
+__global__ void k_nbr_count_ell(K32 k, const float4* HI, RecView LO, const int* cnt, const int* nbr, int* counts) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     const int m = cnt[i] < k.maxn ? cnt[i] : k.maxn;
@@ -1600,7 +1602,7 @@ __global__ void k_nbr_count_ell(K32 k, const float4* HI, const float4* LO, const
 }
 
 template <int DIM>
-__global__ void k_nbr_fill_ell(K32 k, const float4* HI, const float4* LO, const float4* PF, const int* ds,
+__global__ void k_nbr_fill_ell(K32 k, const float4* HI, RecView LO, const float4* PF, const int* ds,
                                const int* ss, const int* cnt, const int* nbr, const int* off, int* list) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
@@ -1621,7 +1623,7 @@ __global__ void k_nbr_fill_ell(K32 k, const float4* HI, const float4* LO, const 
 }
 
 // Largest squared displacement of a real particle since the last list build.
-__global__ void k_disp32(K32 k, const float4* __restrict__ HI, const float4* __restrict__ LO,
+__global__ void k_disp32(K32 k, const float4* __restrict__ HI, RecView LO,
                          const float4* __restrict__ PF, unsigned* __restrict__ maxd) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     float d2 = 0.f;
@@ -1838,7 +1840,8 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     // allocations
     const bool soil = c.solver != 1;
     for (int q = 0; q < 2; ++q) {
-        st->P[q].hi = dal<float4>(*st, n); st->P[q].lo = dal<float4>(*st, n); st->P[q].vel = dal<float4>(*st, n);
+        st->P[q].hi = dal<float4>(*st, n); st->P[q].lo = RecView{dal<float4>(*st, 2 * (size_t)n)};
+        st->P[q].vel = dal<float4>(*st, n);
         st->P[q].drho = dal<float>(*st, n); st->P[q].mass = dal<float>(*st, n); st->P[q].ids = dal<int4>(*st, n);
         if (soil) {
             st->P[q].sig = dal<float>(*st, 6 * (size_t)n); st->P[q].eeq = dal<float>(*st, n);
@@ -1847,7 +1850,9 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
         }
     }
     T32& t = st->T;
-    t.vt = dal<float4>(*st, n); t.pr = dal<float2>(*st, n); t.drt = dal<float>(*st, n); t.dd = dal<float>(*st, n);
+    // v_tmp lives in the second half of the current buffer's records (sorts copy back in place,
+    // so the current buffer is always P[0])
+    t.vt = RecView{st->P[0].lo.p ? st->P[0].lo.p + 1 : nullptr}; t.pr = dal<float2>(*st, n); t.drt = dal<float>(*st, n); t.dd = dal<float>(*st, n);
     t.dv = dal<float4>(*st, n); t.cf = dal<float>(*st, n); t.xs = dal<float4>(*st, n);
     t.L = c.corr == 1 ? dal<float>(*st, 6 * (size_t)n) : nullptr;
     t.cnt = dal<int>(*st, n);
@@ -1891,7 +1896,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     cudaMemcpyAsync(d2, pp->mass, sizeof(double) * n, kind, s);
     cudaMemcpyAsync(d3, pp->m_V, sizeof(double) * n, kind, s);
     cudaMemcpyAsync(d4, pp->pressure, sizeof(double) * n, kind, s);
-    int* imt = reinterpret_cast<int*>(st->P[1].lo);
+    int* imt = reinterpret_cast<int*>(st->P[1].lo.p);
     int* imid = imt + n;
     int* ioid = imid + n;
     int* idyn = reinterpret_cast<int*>(st->P[1].vel);
@@ -1937,7 +1942,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     }
     cudaStreamSynchronize(s);
     cudaMemsetAsync(st->P[1].hi, 0, sizeof(float4) * n, s);
-    cudaMemsetAsync(st->P[1].lo, 0, sizeof(float4) * n, s);
+    cudaMemsetAsync(st->P[1].lo.p, 0, sizeof(float4) * 2 * (size_t)n, s);
     cudaMemsetAsync(st->P[1].vel, 0, sizeof(float4) * n, s);
     // static block: sort once into P[1], copy the whole static block into both buffers
     if (n - nd > 0) {
@@ -1949,7 +1954,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
         const size_t off = nd;
         const size_t ns = n - nd;
         cudaMemcpyAsync(dst.hi + off, src.hi + off, sizeof(float4) * ns, cudaMemcpyDeviceToDevice, s);
-        cudaMemcpyAsync(dst.lo + off, src.lo + off, sizeof(float4) * ns, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(dst.lo.p + 2 * off, src.lo.p + 2 * off, sizeof(float4) * 2 * ns, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(dst.vel + off, src.vel + off, sizeof(float4) * ns, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(dst.drho + off, src.drho + off, sizeof(float) * ns, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(dst.mass + off, src.mass + off, sizeof(float) * ns, cudaMemcpyDeviceToDevice, s);
@@ -2119,7 +2124,7 @@ void f32::rebuild(Fp32State& st, cudaStream_t s, bool in_place) {
 }
 
 void fp32_sort(Fp32State& st, cudaStream_t s) {
-    rebuild(st, s, false);
+    rebuild(st, s, true);  // in place: v_tmp lives in the current buffer's records
     st.lists_valid = true;
     st.built = true;
     ++st.rebuilds;
@@ -2605,9 +2610,10 @@ std::vector<std::pair<void*, size_t>> snap_items(Fp32State& st) {
     const size_t n = st.n;
     P32& p = st.P[st.cur];
     std::vector<std::pair<void*, size_t>> v = {
-        {p.hi, sizeof(float4) * n}, {p.lo, sizeof(float4) * n}, {p.vel, sizeof(float4) * n},
-        {p.drho, sizeof(float) * n}, {p.mass, sizeof(float) * n}, {p.ids, sizeof(int4) * n},
-        {st.T.vt, sizeof(float4) * n}};
+        {p.hi, sizeof(float4) * n}, {p.lo.p, sizeof(float4) * 2 * n}, {p.vel, sizeof(float4) * n},
+        {p.drho, sizeof(float) * n}, {p.mass, sizeof(float) * n}, {p.ids, sizeof(int4) * n}};
+    // (v_tmp, which the mu(I) first loop reads from the previous step for boundary particles,
+    // travels in the second half of the lo records)
     if (p.sig) {
         v.push_back({p.sig, sizeof(float) * 6 * n});
         v.push_back({p.eeq, sizeof(float) * n});

@@ -35,6 +35,22 @@ struct K32 {
     float inv_Q;    // 1 / Q (a power of two)
 };
 
+// The lo record (lx, ly, lz, m_V) and the v_tmp record (v_tmp, p / rho_tmp^2) of a particle
+// sit side by side in one 32-byte record, so the rates pass gathers both of a neighbour with
+// one 256-bit load.  RecView is one half of the interleaved array: element i at p[2 i].
+struct RecView {
+    float4* p;
+    __host__ __device__ __forceinline__ float4& operator[](size_t i) const { return p[2 * i]; }
+};
+// Both halves of neighbour j's record in one read-only 256-bit load (base = the lo view's
+// array; the array is 32-byte aligned and not written by the kernel that calls this).
+__device__ __forceinline__ void ldg_rec(const float4* base, int j, float4& lo, float4& vt) {
+    const float4* a = base + 2 * (size_t)j;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w), "=f"(vt.x), "=f"(vt.y), "=f"(vt.z), "=f"(vt.w)
+        : "l"(a));
+}
+
 // Type word (the w lane of hi): bits 0-15 material type (signed), bit 16 is_dynamic, bits
 // 17-28 scene number of a batched ensemble, bit 30 set (the word stays a normal float).
 __device__ __forceinline__ int tf_type(float w) { return (int)(short)(__float_as_int(w) & 0xffff); }
@@ -207,7 +223,7 @@ __device__ __forceinline__ void delta(const float4& hi_i, const float4& lo_i, co
 // last check) pass use_pf = false.
 template <int DIM, class F>
 __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4* __restrict__ HI,
-                                               const float4* __restrict__ LO, const float4* __restrict__ PF,
+                                               RecView LO, const float4* __restrict__ PF,
                                                const int* __restrict__ dstart, const int* __restrict__ sstart,
                                                bool flow_i, F&& body, bool list_radius = false,
                                                bool use_pf = true) {
@@ -263,9 +279,12 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
 // two gathers overlap; the list's skin pairs load it for nothing).  Two neighbours per trip;
 // the next trip's two list entries are loaded before this trip's gathers, so the entry
 // stream (from DRAM) overlaps the gathers and the maths.
-template <int DIM, bool FB, bool CODE = false, class G, class F>
+// REC: the payload is the neighbour's v_tmp record, loaded together with its lo record in
+// one 256-bit read (ldg_rec) instead of through gather(j) (the overflow traversal still
+// calls gather).
+template <int DIM, bool FB, bool CODE = false, bool REC = false, class G, class F>
 __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
-                                           const float4* __restrict__ HI, const float4* __restrict__ LO,
+                                           const float4* __restrict__ HI, RecView LO,
                                            const float4* __restrict__ PF, const int* __restrict__ dstart,
                                            const int* __restrict__ sstart, bool flow_i, G&& gather, F&& body) {
     if (!FB) {
@@ -290,9 +309,17 @@ __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __res
             int n0 = 0, n1 = 0;
             if (s + 3 < m) { n0 = lp[0]; n1 = lp[stride]; lp += 2 * stride; }
             const int j0 = e0 & kEntryMask, j1 = e1 & kEntryMask;
-            const float4 l0 = LO[j0], l1 = LO[j1];
-            const auto g0 = gather(j0);
-            const auto g1 = gather(j1);
+            float4 l0, l1;
+            decltype(gather(0)) g0, g1;
+            if constexpr (REC) {
+                ldg_rec(LO.p, j0, l0, g0);
+                ldg_rec(LO.p, j1, l1, g1);
+            } else {
+                l0 = LO[j0];
+                l1 = LO[j1];
+                g0 = gather(j0);
+                g1 = gather(j1);
+            }
             // s is even: the slot numbers' low bit is known, so a body's test of the slot
             // (a flush every eight) is decided at compile time for the first of the pair
             visit(e0, l0, g0, s & ~1);
@@ -303,7 +330,13 @@ __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __res
         if (s < m) {
             const int e = nbr[(size_t)s * stride + i];
             const int j = e & kEntryMask;
-            visit(e, LO[j], gather(j), s);
+            if constexpr (REC) {
+                float4 l, g;
+                ldg_rec(LO.p, j, l, g);
+                visit(e, l, g, s);
+            } else {
+                visit(e, LO[j], gather(j), s);
+            }
         }
     } else {
         int s = 0;
@@ -319,7 +352,7 @@ struct NoPayload {};
 // for_nbrs_g without a payload: body(j, d, r2, slot, type_j, m_V_j).
 template <int DIM, bool FB, class F>
 __device__ __forceinline__ void for_nbrs(const K32& k, int i, const int* __restrict__ cnt, const int* __restrict__ nbr,
-                                         const float4* __restrict__ HI, const float4* __restrict__ LO,
+                                         const float4* __restrict__ HI, RecView LO,
                                          const float4* __restrict__ PF, const int* __restrict__ dstart,
                                          const int* __restrict__ sstart, bool flow_i, F&& body) {
     for_nbrs_g<DIM, FB>(k, i, cnt, nbr, HI, LO, PF, dstart, sstart, flow_i, [](int) { return NoPayload{}; },
@@ -373,7 +406,7 @@ struct Ovf {
 // Persistent per-particle state of the FP32-mixed form.
 struct P32 {
     float4* hi;     // (hx, hy, hz, type word)
-    float4* lo;     // (lx, ly, lz, m_V)
+    RecView lo;     // (lx, ly, lz, m_V), first half of the interleaved records
     float4* vel;    // (vx, vy, vz, pressure)
     float* drho;    // density - rho0
     float* mass;
@@ -391,7 +424,7 @@ __device__ __forceinline__ int sym_idx(int a, int b) { return a == b ? a : 2 + a
 
 // ---------------------------------------------------------------- transient state
 struct T32 {
-    float4* vt;     // (v_tmp, p / rho_tmp^2)
+    RecView vt;     // (v_tmp, p / rho_tmp^2), second half of the current buffer's records
     float2* pr;     // (pressure, rho_tmp)
     float* drt;     // rho_tmp - rho0
     float* dd;      // d_density
