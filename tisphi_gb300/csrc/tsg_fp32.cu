@@ -489,13 +489,8 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
         const int ti = tf_type(p.hi[i].w);
         if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
             CSum bv[3], bp, sh;
-            // the neighbour's v_tmp comes with its lo record (one 256-bit read)
-            for_nbrs_g<DIM, FB, false, true>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
-                                             [&](int j) { return t.vt[j]; },
-                                             [&](int j, const float* d, float r2, int sidx, int, float mV,
-                                                 const float4& vt) {
+            auto term = [&](const float* d, float r2, int sidx, float mV, const float4& vt, const float2& pr) {
                 const float w = w_pair<true, false, KT>(k, r2).w;
-                const float2 pr = t.pr[j];
                 const float mw = mV * w;
                 if (SH) sh.p = __fmaf_rn(mV, w, sh.p);
                 bv[0].add(mw * vt.x);
@@ -506,7 +501,17 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
                     bv[0].flush(); bv[1].flush(); bv[2].flush(); bp.flush();
                     if (SH) sh.flush();
                 }
-            });
+            };
+            if (!FB) {  // the neighbour's v_tmp comes with its lo record, (p, rho~) beside it
+                for_list4<DIM>(k, i, t.cnt, t.nbr, p.lo, t.pr,
+                               [&](int, const float* d, float r2, int sidx, float mV, const float4& vt,
+                                   const float2& pr) { term(d, r2, sidx, mV, vt, pr); });
+            } else {
+                for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, false,
+                                  [&](int j, const float* d, float r2, int sidx, int, float mV) {
+                    term(d, r2, sidx, mV, t.vt[j], t.pr[j]);
+                });
+            }
             float f;
             if (SH) {
                 const float sum = sh.get();
@@ -686,14 +691,17 @@ __global__ void k_rigid_rest32(int n, const int* __restrict__ ids_tab, const dou
 // FL: the fluid's CSPM factors (the Shepard factor; with CORR the CSPM matrix too) are
 // computed here, in the same neighbour loop, instead of by the correction kernel (the
 // first rates pass of the step: the particles do not move between the correction and the
-// second pass, which reads them back).  With CORR the continuity sum then runs on the
-// symmetric part of sum_j m_Vj G_j (v_i - v_j) dx_j^T, contracted with the inverse CSPM
-// matrix once the loop has built it: (L (v_i - v_j)) . dx = sum_ab L_ab dv_b dx_a and L is
-// symmetric.
+// second pass, which reads them back).  With CORR the continuity sum of both passes runs
+// on the symmetric part of sum_j m_Vj G_j (v_i - v_j) dx_j^T, contracted after the loop
+// with the inverse CSPM matrix (built by the same loop in the first pass, read back in the
+// second): (L (v_i - v_j)) . dx = sum_ab L_ab dv_b dx_a and L is symmetric, so a neighbour
+// costs six multiply-adds into the tensor instead of L applied to its velocity difference.
 template <int DIM, bool FB, bool CORR, int KT, int REP, bool FL = false>
 __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
                           const int* __restrict__ sstart, Ovf ovf) {
-    constexpr bool FLC = FL && CORR;  // continuity through the CSPM tensor
+    constexpr bool FLC = FL && CORR;  // the CSPM matrix is built in this pass
+    // with CORR both passes sum the continuity tensor and contract it with L after the loop
+    constexpr bool TEN = CORR;
     FOR_PARTICLES(FB, 0, k.nd, ovf, t.cnt, k.maxn, {
       const float wi = p.hi[i].w;
       if (tf_type(wi) == MAT_FLUID) {
@@ -702,11 +710,11 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         const float rti = k.rho0 + t.drt[i];
         const float visc_b = k.rho0 / rti;
         float L[9];
-        if (CORR && !FLC)
+        if (CORR && !TEN)
             load_L(t.L, k.n, i, L);
         CSum dd, dv[3];
         CSum sh;                                 // FL: Shepard sum
-        float A[6] = {0, 0, 0, 0, 0, 0};         // FLC: continuity tensor (symmetric part)
+        float A[6] = {0, 0, 0, 0, 0, 0};         // TEN: continuity tensor (symmetric part)
         float M[6] = {0, 0, 0, 0, 0, 0};         // FLC: CSPM matrix
         const bool rep_on = REP < 0 ? (k.boundary == 3 || k.boundary == 4) : REP == 1;
         // viscosity factor for fluid and for boundary neighbours; -rho0 p_i / rho_i^2
@@ -723,7 +731,7 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
             const float e[3] = {__fmul_rn(mg, d[0]), __fmul_rn(mg, d[1]), __fmul_rn(mg, d[2])};
             // WCSPH scenes hold no soil: the flow neighbours are the fluid ones
             if (FL) cspm_terms<DIM>(sh, M, d, e, wg.w, mVj, cj == kCodeFluid, CORR && cj == kCodeFluid);
-            if (FLC) {
+            if (TEN) {
                 const float dvv[3] = {dvx, dvy, dvz};
                 for (int a = 0; a < DIM; ++a) {
                     A[a] = fmaf(dvv[a], e[a], A[a]);
@@ -761,7 +769,7 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
             if (DIM == 3) dv[2].add(sc * d[2]);
             if (sidx % kFlushEvery == kFlushEvery - 1) {
                 if (FL) sh.flush();
-                if (!FLC) dd.flush();
+                if (!TEN) dd.flush();
                 dv[0].flush(); dv[1].flush(); dv[2].flush();
             }
         });
@@ -777,6 +785,11 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
             ddi = 0.f;
             for (int a = 0; a < DIM; ++a)
                 for (int b = a; b < DIM; ++b) ddi = fmaf(inv[sym_idx(a, b)], A[sym_idx(a, b)], ddi);
+        } else if (TEN) {
+            ddi = 0.f;
+            for (int a = 0; a < DIM; ++a)
+                for (int b = a; b < DIM; ++b)
+                    ddi = fmaf(t.L[(size_t)sym_idx(a, b) * k.n + i], A[sym_idx(a, b)], ddi);
         } else {
             ddi = dd.get();
         }

@@ -85,7 +85,7 @@ __device__ __forceinline__ int make_entry(int j, int tj, int ox, int oy, int oz)
 // Offset field v of an axis as the float v - 1: v in the low mantissa bits of 2^23 gives
 // the float 2^23 + v exactly, and subtracting 2^23 + 1 is exact.
 __device__ __forceinline__ float entry_offset(int e, int axis) {
-    return __int_as_float((int)(0x4B000000u | (((unsigned)e >> (26 + 2 * axis)) & 3u))) - 8388609.f;
+    return __fadd_rn(__int_as_float((int)(0x4B000000u | (((unsigned)e >> (26 + 2 * axis)) & 3u))), -8388609.f);
 }
 // Entry for neighbour j of i from their hi records (list builders without staged offsets).
 __device__ __forceinline__ int entry_of(const K32& k, int j, const float4& hi_i, const float4& hi_j) {
@@ -271,6 +271,16 @@ __device__ __forceinline__ void enum_neighbors(const K32& k, int i, const float4
     }
 }
 
+// x_i - x_j of list entry e (neighbour lo record l) and its square, rounding spelled out
+// once for every traversal.
+template <int DIM>
+__device__ __forceinline__ float list_delta(const K32& k, int e, const float4& lo_i, const float4& l, float* d) {
+    d[0] = __fmaf_rn(entry_offset(e, 0), k.Q, __fadd_rn(lo_i.x, -l.x));
+    d[1] = __fmaf_rn(entry_offset(e, 1), k.Q, __fadd_rn(lo_i.y, -l.y));
+    d[2] = DIM == 3 ? __fmaf_rn(entry_offset(e, 2), k.Q, __fadd_rn(lo_i.z, -l.z)) : 0.f;
+    return dist2<DIM>(d);
+}
+
 // Iterate i's neighbour list (FB = false) or traverse its stencil directly (FB = true: the
 // particle's list overflowed).  body(j, d, r2, slot, type_j, m_V_j, g_j) (with CODE: the
 // neighbour's material code in place of its type) gets the exact f32
@@ -295,10 +305,7 @@ __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __res
         // neighbour record: position difference, type, m_V (lists hold support + skin)
         auto visit = [&](int e, const float4& l, const auto& g, int s) {
             float d[3];
-            d[0] = entry_offset(e, 0) * k.Q + (lo_i.x - l.x);
-            d[1] = entry_offset(e, 1) * k.Q + (lo_i.y - l.y);
-            d[2] = DIM == 3 ? entry_offset(e, 2) * k.Q + (lo_i.z - l.z) : 0.f;
-            const float r2 = dist2<DIM>(d);
+            const float r2 = list_delta<DIM>(k, e, lo_i, l, d);
             const int c = (e >> kEntryBits) & 7;
             if (r2 < k.R2) body(e & kEntryMask, d, r2, s, CODE ? c : class_type(c), l.w, g);
         };
@@ -348,6 +355,50 @@ __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __res
 }
 
 struct NoPayload {};
+
+// i's list (not overflowed) four entries per trip, for the short, latency-bound lists of the
+// boundary pass: each entry's lo + v_tmp record (one 256-bit read) and its extra payload
+// X[j] are loaded for all four entries before the first is used, and the next trip's
+// entries before this trip's gathers.  body(j, d, r2, slot, m_V_j, v_tmp_j, X_j) runs for
+// the entries within the support, in slot order (so sums come out as with one entry per
+// trip).
+template <int DIM, class X, class F>
+__device__ __forceinline__ void for_list4(const K32& k, int i, const int* __restrict__ cnt,
+                                          const int* __restrict__ nbr, RecView LO, const X* __restrict__ XS,
+                                          F&& body) {
+    const int m = cnt[i];
+    const float4 lo_i = LO[i];
+    const size_t stride = (size_t)k.n;
+    const int* lp = nbr + i;
+    int e[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) e[u] = u < m ? lp[(size_t)u * stride] : 0;
+    for (int s = 0; s < m; s += 4) {
+        int nx[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) nx[u] = s + 4 + u < m ? lp[(size_t)(s + 4 + u) * stride] : 0;
+        float4 l[4], g[4];
+        X x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (s + u < m) {
+                const int j = e[u] & kEntryMask;
+                ldg_rec(LO.p, j, l[u], g[u]);
+                x[u] = XS[j];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (s + u < m) {
+                float d[3];
+                const float r2 = list_delta<DIM>(k, e[u], lo_i, l[u], d);
+                if (r2 < k.R2) body(e[u] & kEntryMask, d, r2, s + u, l[u].w, g[u], x[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) e[u] = nx[u];
+    }
+}
 
 // for_nbrs_g without a payload: body(j, d, r2, slot, type_j, m_V_j).
 template <int DIM, bool FB, class F>
