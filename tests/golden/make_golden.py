@@ -50,6 +50,15 @@ def cases():
         # dynamic rigid box on the water surface: the reaction scatter and shape matching
         "wc2d_rigid": (scenes.floating_box_2d(spacing=0.04, water=(0.4, 0.2), box=(0.12, 0.08), box_at=(0.12, 0.2),
                                               domain=(0.8, 0.6), jitter=4e-4, seed=16), 3),
+        # longer horizons: a finer 2D dambreak (200 fluid particles) over 40 leap-frog steps,
+        # the 3D CSPM dambreak at half the spacing (192 fluid) over 3 steps, and the mu(I)
+        # column over 40 steps
+        "wc2d_lf_40": (scenes.dambreak_2d(spacing=0.02, width=0.4, height=0.2, domain=(0.8, 0.6), jitter=2e-4,
+                                          seed=17), 40),
+        "wc3d_cspm_fine": (scenes.dambreak_3d(spacing=0.02, domain=(0.32, 0.24, 0.16), size=(0.16, 0.12, 0.08),
+                                              jitter_frac=0.01, seed=18), 3),
+        "mui2d_40": (scenes.column_2d(method=2, spacing=0.01, width=0.1, height=0.05, domain=(0.2, 0.1),
+                                      seed=19), 40),
     }
 
 
