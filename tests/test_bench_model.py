@@ -33,3 +33,18 @@ def test_boundary_bytes_unchanged_by_fusion():
     a = bench.algorithmic_bytes("boundary", N_TOTAL, N_FLUID, "fp32_mixed", True, LISTS, "lf")
     b = bench.algorithmic_bytes("boundary", N_TOTAL, N_FLUID, "fp32_mixed", True, LISTS)
     assert a == b == 57_381_404
+
+
+def test_traffic_read_from_the_committed_capture():
+    """roofline.traffic: the rates capture's DRAM bytes per launch (profiles/), scaled by the
+    list entries of the run against those of the capture."""
+    traffic, src = bench.read_profile_traffic("rates_fp32_mixed_3d_dambreak", LISTS["entries_real"])
+    assert src["profile"] == "profiles/rates_fp32_mixed_3d_dambreak.md"
+    assert src["capture_list_entries"] > 0 and src["capture_dram_bytes_per_launch"] > 0
+    want = src["capture_dram_bytes_per_launch"] * LISTS["entries_real"] / src["capture_list_entries"]
+    assert abs(traffic - want) <= 1e-6 * want
+    # the measured traffic is within a few percent of the algorithmic bytes of the same launch
+    alg = bench.algorithmic_bytes("rates", N_TOTAL, N_FLUID, "fp32_mixed", True, LISTS, "lf")
+    assert 0.95 < traffic / alg < 1.10
+    missing, why = bench.read_profile_traffic("no_such_kernel", LISTS["entries_real"])
+    assert missing is None and "missing" in why
