@@ -7,7 +7,9 @@
   per-scene mass identical.
 * One batch scene against the f64 oracle with the same tolerances.
 * Graph replay against the eager step path (per-phase profiling forces eager steps):
-  bit-identical, since both launch the same kernels in the same order.
+  bit-identical, since both launch the same kernels in the same order; also one step per
+  call through several list rebuilds (the graph's conditional node against the host's
+  decision).
 * The step sequence (fluid EOS inside init_real2tmp and the leap-frog half step; advect,
   advect_pos and the density clamp in one pass; Shepard factors from the first rates and
   boundary passes instead of the correction kernel) against the reference's stages called
@@ -164,6 +166,31 @@ def test_graph_replay_equals_eager(native):
         cnt = (ctypes.c_int64 * 16)()
         lib.tsg_profile_read(ms, cnt, len(nat.PHASES))
         lib.tsg_profile(0)
+    for nm in ("x", "v", "density", "pressure", "id0"):
+        np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy(), err_msg=nm)
+
+
+def test_single_step_replays_through_rebuilds_equal_eager(native):
+    """step() one step at a time (a graph replay per call, its list rebuilds taken by the
+    graph's conditional node) through several list rebuilds: bit-identical to eager steps,
+    which decide each rebuild on the host."""
+    from tisphi_gb300 import _native as nat
+    lib = nat.load()
+    d = small_dambreak_2d()
+    a, b = _single(d), _single(d)
+    for _ in range(300):
+        a.solver.step()
+    lib.tsg_profile(1)
+    try:
+        for _ in range(300):
+            b.solver.step()
+    finally:
+        ms = (ctypes.c_double * 16)()
+        cnt = (ctypes.c_int64 * 16)()
+        lib.tsg_profile_read(ms, cnt, len(nat.PHASES))
+        lib.tsg_profile(0)
+    ba, bb = a.ps.list_stats()["builds"], b.ps.list_stats()["builds"]
+    assert ba == bb and ba >= 3, (ba, bb)
     for nm in ("x", "v", "density", "pressure", "id0"):
         np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy(), err_msg=nm)
 

@@ -1443,9 +1443,10 @@ struct ExportSet {
     int comps[8];
     size_t off[8];
 };
-__global__ void k_export_set(K32 k, P32 p, T32 t, ExportSet es, double* out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) return;
+// Particles [i0, i1) of the fields in es, row-major per field into out + es.off[q].
+__global__ void k_export_set(K32 k, P32 p, T32 t, ExportSet es, double* out, int i0, int i1) {
+    int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= i1) return;
     for (int q = 0; q < es.count; ++q)
         export_one(k, p, t, es.what[q], i, out + es.off[q] + (size_t)i * es.comps[q], 1);
 }
@@ -2002,6 +2003,9 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
 
 void fp32_destroy(Fp32State* st) {
     if (!st) return;
+    for (auto& e : st->copy_ev)
+        if (e) cudaEventDestroy(e);
+    if (st->copy_stream) cudaStreamDestroy(st->copy_stream);
     for (auto& g : st->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     if (st->snap) cudaFree(st->snap);
@@ -2916,6 +2920,18 @@ int fp32_write(Fp32State& st, const char* name, const void* src, bool from_devic
     return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;
 }
 
+// The copy stream and events of the chunked export, created on first use.
+static bool export_pipe(Fp32State& st) {
+    if (st.copy_stream) return true;
+    if (cudaStreamCreateWithFlags(&st.copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        st.copy_stream = nullptr;
+        return false;
+    }
+    for (auto& e : st.copy_ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+    return true;
+}
+
 int fp32_read_set(Fp32State& st, int count, const char* const* names, void* const* dsts, int mode,
                   cudaStream_t s) {
     if (count <= 0 || count > 8) return TSG_E_ARG;
@@ -2936,11 +2952,31 @@ int fp32_read_set(Fp32State& st, int count, const char* const* names, void* cons
             const int rc = fp32_read(st, names[q], dsts[q], mode == 0 ? 2 : mode, s);
             if (rc) return rc;
         }
-    } else {
+    } else if (mode == 1 || !export_pipe(st)) {
         const cudaMemcpyKind kind = mode == 1 ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-        TSG_LAUNCH(k_export_set, nblk(n), TPB, s, st.k, st.P[st.cur], st.T, es, st.stage);
+        TSG_LAUNCH(k_export_set, nblk(n), TPB, s, st.k, st.P[st.cur], st.T, es, st.stage, 0, (int)n);
         for (int q = 0; q < count; ++q)
             cudaMemcpyAsync(dsts[q], st.stage + es.off[q], sizeof(double) * es.comps[q] * n, kind, s);
+    } else {
+        // host destinations: the conversion runs chunk by chunk on s and each chunk's copies
+        // on the copy stream, so the host link (the bound) starts after the first chunk
+        constexpr int C = 4;
+        for (int c = 0; c < C; ++c) {
+            const size_t i0 = n * c / C, i1 = n * (c + 1) / C;
+            if (i1 > i0)
+                TSG_LAUNCH(k_export_set, nblk(i1 - i0), TPB, s, st.k, st.P[st.cur], st.T, es, st.stage, (int)i0,
+                           (int)i1);
+            cudaEventRecord(st.copy_ev[c], s);
+            cudaStreamWaitEvent(st.copy_stream, st.copy_ev[c], 0);
+            for (int q = 0; q < count; ++q) {
+                const size_t a = (size_t)es.comps[q] * i0, b = (size_t)es.comps[q] * i1;
+                if (b > a)
+                    cudaMemcpyAsync(static_cast<double*>(dsts[q]) + a, st.stage + es.off[q] + a,
+                                    sizeof(double) * (b - a), cudaMemcpyDeviceToHost, st.copy_stream);
+            }
+        }
+        cudaEventRecord(st.copy_ev[C], st.copy_stream);
+        cudaStreamWaitEvent(s, st.copy_ev[C], 0);
     }
     if (mode == 0) cudaStreamSynchronize(s);
     return cudaGetLastError() == cudaSuccess ? 0 : TSG_E_CUDA;

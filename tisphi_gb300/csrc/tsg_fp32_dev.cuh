@@ -644,6 +644,9 @@ struct Fp32State {
     long long body_kernels = 0;   // kernel nodes of one rebuild body
     int* d_rebuilds = nullptr;    // rebuilds taken by graph replays (device counter)
     int rebuilds_seen = 0;        // part of d_rebuilds already folded into the counters
+    // field export to host memory: conversion of one chunk overlaps the copy of the one before
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_ev[5] = {};
     void* snap = nullptr;         // autotuner snapshot of the particle state
     void* adj = nullptr;          // adjoint work buffers (tsg_adjoint.cu)
 };
