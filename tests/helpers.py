@@ -49,3 +49,28 @@ def rel_err(a, b, floor=0.0):
     with np.errstate(divide="ignore", invalid="ignore"):
         r = np.where(scale > 0, np.abs(a - b) / scale, np.abs(a - b))
     return float(np.nanmax(r)) if r.size else 0.0
+
+
+def write_box_obj(path, size=(1.0, 1.0, 1.0)):
+    """A closed box [0, size] as a Wavefront OBJ file: eight corners, six quads."""
+    sx, sy, sz = size
+    corners = [(x, y, z) for x in (0.0, sx) for y in (0.0, sy) for z in (0.0, sz)]
+    # corner index = 4 * ix + 2 * iy + iz (1-based in the file), quads wound outwards
+    quads = [(1, 2, 4, 3), (5, 7, 8, 6), (1, 5, 6, 2), (3, 4, 8, 7), (1, 3, 7, 5), (2, 6, 8, 4)]
+    with open(path, "w") as f:
+        for c in corners:
+            f.write("v %r %r %r\n" % c)
+        for q in quads:
+            f.write("f " + " ".join(f"{k}/{k}/{k}" for k in q) + "\n")
+    return str(path)
+
+
+def mesh_box_scene_3d(obj_path, box_density=500.0, steps_dt=2e-5):
+    """floating_box_3d with the rigid box given as a mesh body (a unit-box OBJ scaled to
+    0.1 x 0.06 x 0.08 m) instead of a block."""
+    d = scenes.floating_box_3d(dt=steps_dt, box_density=box_density)
+    d["Blocks"] = [b for b in d["Blocks"] if b["objectId"] != 1]
+    d["Bodies"] = [{"objectId": 1, "geometryFile": obj_path, "translation": [0.1, 0.2, 0.04],
+                    "scale": [0.1, 0.06, 0.08], "rotationAngle": 0.0, "rotationAxis": [0.0, 0.0, 1.0],
+                    "velocity": [0.0, 0.0, 0.0], "materialId": 1, "isDynamic": True}]
+    return d

@@ -7,15 +7,21 @@ that scatter, and replace ti.polar_decompose by the same scaled Newton iteration
 form is bit-identical to the oracle (the golden fixture wc2d_rigid pins the oracle to the
 reference's own rigid-body code run under the Taichi emulator).  Cases: a 2D water column
 with a floating box (leap-frog over 300 steps, symplectic Euler + XSPH), a sinking box, the
-3D counterpart with CSPM, and a mu(I) column with a box resting on the sand.  The FP32-mixed
+3D counterpart with CSPM (also with the box given as a mesh body), and a mu(I) column with a
+box resting on the sand.  The FP32-mixed
 WCSPH form takes them too (reaction gathered over each rigid particle's list, shape matching
 in f64 on its hi + lo positions), within its tolerances against the oracle; granular scenes
 with dynamic rigid bodies take the FP64 form.
 """
+import os
+import tempfile
+
 import numpy as np
 import pytest
 
-from helpers import cfg_of, describe_diff, small_column
+from helpers import cfg_of, describe_diff, mesh_box_scene_3d, small_column, write_box_obj
+
+_OBJ_DIR = tempfile.mkdtemp(prefix="tsg_mesh_")
 
 pytestmark = pytest.mark.gpu
 
@@ -49,6 +55,8 @@ def _cases():
         "2d_sink": (scenes.floating_box_2d(box_density=3000.0, box_at=(0.3, 0.45)), 200),
         "3d_cspm": (scenes.floating_box_3d(), 20),
         "mui_box_on_sand": (_box_on_sand(), 100),
+        # the box as a mesh body (a unit-box OBJ voxelised at the particle diameter)
+        "3d_mesh_body": (mesh_box_scene_3d(write_box_obj(os.path.join(_OBJ_DIR, "unit_box.obj"))), 20),
     }
 
 
@@ -102,7 +110,7 @@ def _by_id(ps_ids, v):
     return out
 
 
-@pytest.mark.parametrize("name", ["2d_lf_float", "2d_sink", "3d_cspm"])
+@pytest.mark.parametrize("name", ["2d_lf_float", "2d_sink", "3d_cspm", "3d_mesh_body"])
 def test_rigid_fp32_mixed_close(oracle_lib, native, name):
     """The FP32-mixed WCSPH form with dynamic rigid bodies against the oracle: fluid density
     within 1e-5 relative, every position within 2e-6 m, the rigid particles' accelerations

@@ -165,8 +165,19 @@ def build_scene(cfg, geom: SceneGeometry = None) -> SceneArrays:
             is_dynamic, color)
         object_counts[block["objectId"]] = pts.shape[0]
 
-    if cfg.get_bodies():
-        raise NotImplementedError("mesh bodies (trimesh voxelisation) are not supported")
+    # mesh bodies (eng/particle_system.py:82-91, :175-200): voxelised at the particle diameter
+    for body in cfg.get_bodies() or []:
+        if g.dim != 3:
+            raise NotImplementedError("mesh bodies need a 3D scene (the voxel grid is 3D)")
+        from .mesh_body import load_body
+        mat = get_material(mats, body["materialId"])
+        mat_type = mat["matType"]
+        is_dynamic = bool(body["isDynamic"]) if mat_type > 10 else True
+        pts = load_body(body, g.particle_diameter, base_dir=getattr(cfg, "base_dir", None))
+        color = np.array([c / 255 for c in mat["color"]], dtype=np.float32)
+        add(pts, body.get("velocity", [0.0, 0.0, 0.0]), mat["density0"], body["materialId"], mat_type,
+            body["objectId"], is_dynamic, color)
+        object_counts[body["objectId"]] = pts.shape[0]
 
     if flag_boundary in (BDY_DUMMY, BDY_DUMMY_REP):
         for lo, hi in calc_dummy_boundary(g.dim, g.domain_start, g.domain_end, g.vdomain_start, g.vdomain_end):
