@@ -361,6 +361,12 @@ __global__ void k_bdy(Consts c, Persist64 p, Trans64 t, const int* __restrict__ 
         t.d_density[i] = 0.0;
         const bool dyn = p.is_dynamic[i] != 0;
         for (int d = 0; d < 3; ++d) t.d_vel[(size_t)d * n + i] = dyn ? c.g[d] : 0.0;
+    } else {
+        // dummy / repulsive particles have no rates: zero, as in the reference, where each
+        // particle's never-written rates travel with it through the sort (the rate arrays
+        // here are not reordered, so a slot may hold another particle's)
+        t.d_density[i] = 0.0;
+        for (int d = 0; d < 3; ++d) t.d_vel[(size_t)d * n + i] = 0.0;
     }
 }
 
