@@ -101,3 +101,35 @@ def test_two_dimensional_scene_rejects_bodies(tmp_path):
                     "materialId": 1, "isDynamic": True}]
     with pytest.raises(NotImplementedError):
         build_scene(cfg_of(d))
+
+
+def _stl_ascii(path, v, f):
+    with open(path, "w") as out:
+        out.write("solid box\n")
+        for t in f:
+            out.write("  facet normal 0 0 0\n    outer loop\n")
+            for k in t:
+                out.write("      vertex %.17g %.17g %.17g\n" % tuple(v[k]))
+            out.write("    endloop\n  endfacet\n")
+        out.write("endsolid box\n")
+
+
+def _stl_binary(path, v, f):
+    rec = np.zeros(len(f), dtype=[("normal", "<f4", 3), ("v", "<f4", (3, 3)), ("attr", "<u2")])
+    rec["v"] = v[f]
+    with open(path, "wb") as out:
+        out.write(b"binary box".ljust(80, b" "))
+        out.write(np.uint32(len(f)).tobytes())
+        out.write(rec.tobytes())
+
+
+def test_stl_ascii_and_binary_voxelise_like_obj(tmp_path):
+    v, f = mesh_body.load_obj(write_box_obj(tmp_path / "box.obj", (0.1, 0.06, 0.08)))
+    want = mesh_body.voxel_points(v, f, 0.02)
+    _stl_ascii(tmp_path / "a.stl", v, f)
+    _stl_binary(tmp_path / "b.stl", v, f)
+    for name in ("a.stl", "b.stl"):
+        vs, fs = mesh_body.load_mesh(str(tmp_path / name))
+        assert fs.shape == (12, 3)
+        got = mesh_body.voxel_points(vs, fs, 0.02)
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-9)  # binary STL holds f32 coordinates

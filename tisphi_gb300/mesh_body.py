@@ -7,7 +7,8 @@ vertices.mean(axis=-1)))``, ``voxelized(pitch=particle_diameter).fill()`` and ta
 voxel centres plus the body's translation.  This module restates those steps:
 
 * Wavefront OBJ geometry (``v`` and ``f`` records; polygons split into a fan of triangles
-  from their first vertex; ``a/b/c`` references and negative indices resolved);
+  from their first vertex; ``a/b/c`` references and negative indices resolved) or STL
+  (ASCII or binary);
 * the rotation about an axis through a point (Rodrigues' formula as a 4 x 4 homogeneous
   matrix).  The reference passes ``vertices.mean(axis=-1)`` as the point: the mean of each
   vertex's three coordinates, of which the rotation takes the first three values.  That is
@@ -51,6 +52,34 @@ def load_obj(path):
     if fa.size and (fa.min() < 0 or fa.max() >= len(v)):
         raise ValueError(f"{path}: face references a missing vertex")
     return v, fa
+
+
+def load_stl(path):
+    """(vertices (3F, 3) float64, triangles (F, 3) int64) of an STL file, ASCII or binary
+    (each triangle keeps its own three vertices)."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:5].lower() == b"solid" and b"facet" in data[:1024]:
+        pts = [[float(c) for c in line.split()[1:4]] for line in data.decode("ascii", "replace").splitlines()
+               if line.strip().startswith("vertex")]
+        v = np.asarray(pts, dtype=np.float64).reshape(-1, 3)
+    else:
+        n = int(np.frombuffer(data[80:84], dtype="<u4")[0])
+        rec = np.dtype([("normal", "<f4", 3), ("v", "<f4", (3, 3)), ("attr", "<u2")])
+        if len(data) < 84 + n * rec.itemsize:
+            raise ValueError(f"{path}: truncated binary STL")
+        tri = np.frombuffer(data[84:84 + n * rec.itemsize], dtype=rec)
+        v = tri["v"].reshape(-1, 3).astype(np.float64)
+    if len(v) % 3:
+        raise ValueError(f"{path}: vertex count not a multiple of three")
+    return v, np.arange(len(v), dtype=np.int64).reshape(-1, 3)
+
+
+def load_mesh(path):
+    """OBJ or STL geometry by the file's extension."""
+    if str(path).lower().endswith(".stl"):
+        return load_stl(path)
+    return load_obj(path)
 
 
 def rotation_matrix(angle, direction, point=None):
@@ -134,7 +163,7 @@ def load_body(body, pitch, base_dir=None):
     path = body["geometryFile"]
     if base_dir is not None and not os.path.isabs(path) and not os.path.exists(path):
         path = os.path.join(base_dir, path)
-    v, f = load_obj(path)
+    v, f = load_mesh(path)
     v = v * np.asarray(body.get("scale", 1.0), dtype=np.float64)
     angle = float(body.get("rotationAngle", 0.0)) / 180 * math.pi
     axis = body.get("rotationAxis", [0.0, 0.0, 1.0])
