@@ -59,6 +59,12 @@ def cases():
                                               jitter_frac=0.01, seed=18), 3),
         "mui2d_40": (scenes.column_2d(method=2, spacing=0.01, width=0.1, height=0.05, domain=(0.2, 0.1),
                                       seed=19), 40),
+        # Drucker-Prager with the reference sand scene's integrator (leap-frog + XSPH) and
+        # RK4 over longer horizons
+        "dp2d_lf_xsph_40": (scenes.column_2d(method=3, spacing=0.01, width=0.1, height=0.05, domain=(0.2, 0.1),
+                                             seed=20, integration=2, xsph=True), 40),
+        "wc2d_rk4_20": (scenes.dambreak_2d(spacing=0.02, width=0.4, height=0.2, domain=(0.8, 0.6), jitter=2e-4,
+                                           seed=21, integration=4), 20),
     }
 
 
