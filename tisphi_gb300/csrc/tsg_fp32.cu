@@ -32,6 +32,8 @@
 //
 // Reference: eng/particle_system.py:228-269 (cell list), eng/solver_sph_base.py:41-238,
 // :363-423, :648-669 (step, CSPM, boundary), eng/solver_sph_wc.py:82-132 (WCSPH).
+#include <type_traits>
+
 #include "tsg_fp32_dev.cuh"
 #include "tsg_polar.cuh"
 
@@ -712,7 +714,10 @@ __global__ void __launch_bounds__(256, 4) k_rates32(K32 k, P32 p, T32 t, const f
         float L[9];
         if (CORR && !TEN)
             load_L(t.L, k.n, i, L);
-        CSum dd, dv[3];
+        // the first pass of a leap-frog step with CSPM sets only the half step's velocity
+        // from its accelerations: plain sums there (the step's update takes the second's)
+        CSum dd;
+        typename std::conditional<FLC, PSum, CSum>::type dv[3];
         CSum sh;                                 // FL: Shepard sum
         float A[6] = {0, 0, 0, 0, 0, 0};         // TEN: continuity tensor (symmetric part)
         float M[6] = {0, 0, 0, 0, 0, 0};         // FLC: CSPM matrix

@@ -111,6 +111,14 @@ struct CSum {
     __device__ __forceinline__ float get() { flush(); return s; }
 };
 
+// A plain f32 sum with CSum's interface (flush does nothing).
+struct PSum {
+    float p = 0.f;
+    __device__ __forceinline__ void add(float x) { p += x; }
+    __device__ __forceinline__ void flush() {}
+    __device__ __forceinline__ float get() { return p; }
+};
+
 __device__ __forceinline__ void atomic_max_d(double* addr, double v) {
     unsigned long long* a = reinterpret_cast<unsigned long long*>(addr);
     unsigned long long old = *a;
