@@ -490,7 +490,10 @@ __global__ void k_bdy32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, cons
     FOR_PARTICLES_ACT(FB, base, act ? base : lim, act, nact, lim, ovf, t.cnt, k.maxn, {
         const int ti = tf_type(p.hi[i].w);
         if (ti == MAT_DUMMY || ti == MAT_REP || ti == MAT_RIGID) {
-            CSum bv[3], bp, sh;
+            // plain sums for the extrapolated velocity and pressure (read by this pass only);
+            // the Shepard sum keeps the correction kernel's compensated form
+            PSum bv[3], bp;
+            CSum sh;
             auto term = [&](const float* d, float r2, int sidx, float mV, const float4& vt, const float2& pr) {
                 const float w = w_pair<true, false, KT>(k, r2).w;
                 const float mw = mV * w;
