@@ -8,10 +8,13 @@ cell-sorted blocks, so every comparison matches particles through id0.  Toleranc
 * single-step rates (CSPM factor, d_density, d_vel): normwise relative error <= 1e-4;
 * density after a few steps: relative error <= 1e-5 (the headline accuracy bound);
 * positions after a few steps: absolute error <= 1e-6 m;
-* granular columns (mu(I), Drucker-Prager): single-step d_density, d_vel, stress_tmp and
-  d_stress normwise <= 1e-4; after 20 steps density <= 1e-5 relative, positions <= 1e-7 m,
-  stress normwise <= 1e-4 and the return-mapping case flag equal for >= 99 % of particles
-  (the flag thresholds f = +-1e-4 Pa sit at the f32 resolution of ~2 kPa stresses).
+* granular columns (mu(I), Drucker-Prager, with and without CSPM): single-step d_density,
+  d_vel and stress_tmp normwise <= 1e-4, d_stress within 1e-4 of its largest entry for all
+  but 2 % of the particles (the rest within 2e-2); after 20 steps density <= 1e-5 relative,
+  positions <= 1e-7 m, stress normwise <= 1e-4 (Drucker-Prager: per particle, as d_stress)
+  and the return-mapping case flag equal for >= 99 % of particles (the plastic-branch
+  thresholds, f = +-1e-4 Pa and sqrt(J2) = 1e-8 Pa, sit at or below the f32 resolution of
+  ~2 kPa stresses).
 """
 import numpy as np
 import pytest
@@ -169,9 +172,9 @@ def test_fp32_determinism(oracle_lib, native):
         np.testing.assert_array_equal(a.ps.field(nm).cpu().numpy(), b.ps.field(nm).cpu().numpy())
 
 
-@pytest.mark.parametrize("method", [2, 3])
-def test_soil_one_step_rates_close(oracle_lib, native, method):
-    sim, orc = _pair(small_column(method), oracle_lib)
+@pytest.mark.parametrize("method,corr", [(2, 0), (3, 0), (2, 1), (3, 1)])
+def test_soil_one_step_rates_close(oracle_lib, native, method, corr):
+    sim, orc = _pair(small_column(method, corr=corr), oracle_lib)
     _advance(sim, orc, oracle_lib, 3)
     sim.ps.initialize_particle_system()
     orc.sort()
@@ -182,15 +185,28 @@ def test_soil_one_step_rates_close(oracle_lib, native, method):
     sim.solver.one_step()
     orc.call(oracle_lib.ORC_ONE_STEP)
     f = orc.get("mat_type") == 2
-    names = ["d_density", "d_vel", "stress_tmp"] + (["d_stress"] if method == 3 else [])
+    names = ["d_density", "d_vel", "stress_tmp"]
     errs = {nm: _normwise(_by_id(sim, orc, nm)[f], orc.get(nm)[f]) for nm in names}
     assert all(e < 1e-4 for e in errs.values()), f"normwise errors {errs}"
+    if method == 3:
+        # Drucker-Prager stress rate per particle: the plastic branch needs sqrt(J2) > 1e-8 Pa
+        # (eng/solver_sph_dp.py:194), a threshold far below the f32 resolution of kPa
+        # stresses.  A particle whose stress is zero up to rounding (the free surface:
+        # sqrt(J2) ~ 1e-16 Pa in f64, ~1e-7 Pa in f32) can take the plastic branch in one form
+        # and not the other (with CSPM, two of this column's 1,250 particles at step 3); the
+        # bound holds for all but 2 % of the particles, and those stay within 2e-2
+        ds, ds_o = _by_id(sim, orc, "d_stress")[f], orc.get("d_stress")[f]
+        e_p = np.abs(ds - ds_o).reshape(ds.shape[0], -1).max(axis=1) / np.abs(ds_o).max()
+        off = float(np.mean(e_p >= 1e-4))
+        assert off <= 2e-2 and e_p.max() < 2e-2, f"d_stress: {off:.4f} of particles off, max {e_p.max():.3e}"
 
 
-@pytest.mark.parametrize("method,ti,skin", [(2, 1, 0.05), (3, 1, 0.05), (3, 2, 0.05), (3, 2, 0.1),
-                                             (2, 4, 0.05), (3, 4, 0.05)])
-def test_soil_steps_close(oracle_lib, native, method, ti, skin):
-    """20 steps of mu(I) / Drucker-Prager against the f64 oracle.
+@pytest.mark.parametrize("method,ti,skin,corr", [(2, 1, 0.05, 0), (3, 1, 0.05, 0), (3, 2, 0.05, 0), (3, 2, 0.1, 0),
+                                                  (2, 4, 0.05, 0), (3, 4, 0.05, 0), (2, 1, 0.05, 1),
+                                                  (3, 2, 0.05, 1)])
+def test_soil_steps_close(oracle_lib, native, method, ti, skin, corr):
+    """20 steps of mu(I) / Drucker-Prager against the f64 oracle (corr = 1: with the CSPM
+    gradient correction).
 
     Density and positions within 1e-5 / 1e-7, stress within 1e-4 of its largest entry.  The
     Drucker-Prager stress rate switches its plastic term on where the previous yield value
@@ -200,7 +216,7 @@ def test_soil_steps_close(oracle_lib, native, method, ti, skin):
     11, and its neighbours' stress rates follow it; with skin 0.1, none within the 20 steps).
     For Drucker-Prager the stress bound therefore holds for all but 2 % of the particles, and
     those stay within 2e-2."""
-    d = small_column(method, integration=ti)
+    d = small_column(method, integration=ti, corr=corr)
     d["Configuration"]["neighbourSkin"] = skin
     sim, orc = _pair(d, oracle_lib)
     _advance(sim, orc, oracle_lib, 20)

@@ -375,7 +375,8 @@ int upload_impl(tsg_handle* h, const tsg_particles* p, int from_device, void* st
         Rigid64& rb = h->rigid;
         rb.nobj = (int)robjs.ids.size();
         if ((rc = dalloc(h, &rb.obj_id, robjs.ids.size())) || (rc = dalloc(h, &rb.off, robjs.off.size())) ||
-            (rc = dalloc(h, &rb.rest_cm, 3 * robjs.ids.size())) || (rc = dalloc(h, &rb.list, (size_t)nrdyn)))
+            (rc = dalloc(h, &rb.rest_cm, 3 * robjs.ids.size())) || (rc = dalloc(h, &rb.list, (size_t)nrdyn)) ||
+            (rc = dalloc(h, &rb.scratch, rlist_scratch_ints(h->n, rb.nobj))))
             return rc;
         cudaMemcpy(rb.obj_id, robjs.ids.data(), sizeof(int) * robjs.ids.size(), cudaMemcpyHostToDevice);
         cudaMemcpy(rb.off, robjs.off.data(), sizeof(int) * robjs.off.size(), cudaMemcpyHostToDevice);

@@ -36,6 +36,7 @@
 
 #include "tsg_fp32_dev.cuh"
 #include "tsg_polar.cuh"
+#include "tsg_rigid_list.cuh"
 
 namespace tsg {
 
@@ -582,87 +583,207 @@ __global__ void k_rigid_reaction32(K32 k, P32 p, T32 t, const float4* __restrict
     t.dv[i] = dv;
 }
 
-// Shape matching of one dynamic rigid object per block (eng/solver_sph_base.py:478-511):
-// the object's particles listed in ascending order, then in f64 by one thread the centre of
-// mass, A = sum (m_V rho p) q^T with p = x - cm and q = x0 - rest cm (q kept per id0), its
-// orthogonal polar factor R (identity when every entry is below 1e-8), and every particle
-// moved to cm + R q (its lo record takes the change; hi, a multiple of the list quantum,
-// stays until the next list build).
-__global__ void __launch_bounds__(1024) k_shape_match32(K32 k, P32 p, const int* __restrict__ ids_tab,
-                                                       const int* __restrict__ off, int* __restrict__ lists,
-                                                       const double* __restrict__ qtab) {
-    const int o = blockIdx.x;
-    const int oid = ids_tab[o];
-    int* list = lists + off[o];
-    __shared__ int warp_tot[32];
-    __shared__ int base_s;
-    __shared__ double cm_s[3], R_s[9];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (threadIdx.x == 0) base_s = 0;
+// Object slot of a dynamic rigid particle (-1 for any other), for the list builder: from
+// the type word and object id of the current (sorted) arrays ...
+struct RigidSlot32 {
+    const float4* hi;
+    const int4* ids;
+    const int* tab;
+    int nobj;
+    __device__ int operator()(int i) const {
+        const float w = hi[i].w;
+        if (tf_type(w) != MAT_RIGID || !tf_dyn(w)) return -1;
+        const int id = ids[i].z;
+        for (int o = 0; o < nobj; ++o)
+            if (tab[o] == id) return o;
+        return -1;
+    }
+};
+// ... and from the uploaded arrays (upload order, before the first sort).
+struct RigidSlotUpload {
+    const int* mt;
+    const int* dyn;
+    const int* oid;
+    const int* tab;
+    int nobj;
+    __device__ int operator()(int i) const {
+        if (mt[i] != MAT_RIGID || !dyn[i]) return -1;
+        const int id = oid[i];
+        for (int o = 0; o < nobj; ++o)
+            if (tab[o] == id) return o;
+        return -1;
+    }
+};
+
+// The rigid-object sums of this form run in f64 over the object's list, spread over the
+// GPU: the list is cut into chunks of kRigidChunk entries, one block per (chunk, object);
+// each thread sums a fixed strided share of its chunk in list order, a pairwise tree over
+// the block's threads (stride halving) gives the chunk's partial sums, and one block per
+// object adds the partials in the same way.  The result depends only on the inputs and
+// these fixed shapes (deterministic, not the serial order of the FP64 form).
+constexpr int kRigidBlock = 256;
+constexpr int kRigidChunk = 4 * kRigidBlock;
+template <int NV>
+__device__ __forceinline__ void block_sum_fixed(const double* v, double (*red)[kRigidBlock]) {
+    for (int e = 0; e < NV; ++e) red[e][threadIdx.x] = v[e];
     __syncthreads();
-    for (int i0 = 0; i0 < k.nd; i0 += blockDim.x) {
-        const int i = i0 + threadIdx.x;
-        bool on = false;
-        if (i < k.nd) {
-            const float w = p.hi[i].w;
-            on = tf_type(w) == MAT_RIGID && tf_dyn(w) && p.ids[i].z == oid;
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, on);
-        if (lane == 0) warp_tot[wid] = __popc(bal);
-        __syncthreads();
-        int before = 0, total = 0;
-        for (int w = 0; w < nw; ++w) {
-            if (w < wid) before += warp_tot[w];
-            total += warp_tot[w];
-        }
-        if (on) list[base_s + before + __popc(bal & ((1u << lane) - 1u))] = i;
-        __syncthreads();
-        if (threadIdx.x == 0) base_s += total;
+    for (int w = kRigidBlock / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int e = 0; e < NV; ++e) red[e][threadIdx.x] += red[e][threadIdx.x + w];
         __syncthreads();
     }
-    const int m = base_s;
-    if (threadIdx.x == 0) {
-        double cm[3] = {0.0, 0.0, 0.0}, sum_m = 0.0;
-        for (int q = 0; q < m; ++q) {
-            const int i = list[q];
-            const float4 h = p.hi[i], l = p.lo[i];
+}
+
+// Shape matching of the dynamic rigid objects (eng/solver_sph_base.py:478-511), over each
+// object's list (rebuilt before every shape matching), in three passes:
+//   PASS 0: per chunk, sum m x and m (the centre of mass, calc_cm :502-511);
+//   PASS 1: per chunk, sum A = sum (m_V rho p) q^T with p = x - cm, q = x0 - rest cm (q kept
+//           per id0);
+// each followed by k_rigid_reduce32, and then k_rigid_move32 moves every particle to
+// cm + R q with R the orthogonal polar factor of A (identity when every entry is below
+// 1e-8); its lo record takes the change, hi (a multiple of the list quantum) stays until
+// the next list build.
+template <int PASS>
+__global__ void __launch_bounds__(kRigidBlock) k_rigid_part32(K32 k, P32 p, const int* __restrict__ off,
+                                                             const int* __restrict__ lists,
+                                                             const double* __restrict__ qtab,
+                                                             const double* __restrict__ cm, double* __restrict__ part) {
+    __shared__ double red[PASS == 0 ? 4 : 9][kRigidBlock];
+    const int o = blockIdx.y, c = blockIdx.x;
+    const int m = off[o + 1] - off[o];
+    const int q0 = c * kRigidChunk;
+    if (q0 >= m) return;  // the whole block: no barrier is left half-reached
+    const int* list = lists + off[o];
+    const int q1 = min(m, q0 + kRigidChunk);
+    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int q = q0 + threadIdx.x; q < q1; q += kRigidBlock) {
+        const int i = list[q];
+        const float4 h = p.hi[i], l = p.lo[i];
+        const double x[3] = {k.vs[0] + ((double)h.x + (double)l.x), k.vs[1] + ((double)h.y + (double)l.y),
+                             k.vs[2] + ((double)h.z + (double)l.z)};
+        if (PASS == 0) {
             const double mi = p.mass[i];
-            cm[0] += mi * (k.vs[0] + ((double)h.x + (double)l.x));
-            cm[1] += mi * (k.vs[1] + ((double)h.y + (double)l.y));
-            cm[2] += mi * (k.vs[2] + ((double)h.z + (double)l.z));
-            sum_m += mi;
-        }
-        for (int d = 0; d < 3; ++d) cm[d] /= sum_m;
-        double A[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int q = 0; q < m; ++q) {
-            const int i = list[q];
-            const float4 h = p.hi[i], l = p.lo[i];
+            for (int d = 0; d < 3; ++d) v[d] += mi * x[d];
+            v[3] += mi;
+        } else {
             const double sc = (double)l.w * ((double)k.rho0 + (double)p.drho[i]);
             const double* qq = qtab + 3 * (size_t)p.ids[i].x;
-            const double sp[3] = {sc * ((k.vs[0] + ((double)h.x + (double)l.x)) - cm[0]),
-                                  sc * ((k.vs[1] + ((double)h.y + (double)l.y)) - cm[1]),
-                                  sc * ((k.vs[2] + ((double)h.z + (double)l.z)) - cm[2])};
+            const double sp[3] = {sc * (x[0] - cm[3 * o]), sc * (x[1] - cm[3 * o + 1]), sc * (x[2] - cm[3 * o + 2])};
             for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) A[3 * a + b] += sp[a] * qq[b];
+                for (int b = 0; b < 3; ++b) v[3 * a + b] += sp[a] * qq[b];
         }
-        double R[9];
-        polar3(A, R);
+    }
+    block_sum_fixed<PASS == 0 ? 4 : 9>(v, red);
+    if (threadIdx.x == 0)
+        for (int e = 0; e < 9; ++e) part[((size_t)o * gridDim.x + c) * 9 + e] = e < (PASS == 0 ? 4 : 9) ? red[e][0] : 0.0;
+}
+
+// Orthogonal polar factor for this form's shape matching.  A 2D body (zero third row and
+// column) in closed form: for A2 = [[a, b], [c, d]] = U P with det A2 > 0, U is the rotation
+// by atan2(c - b, a + d), since tr(U P) = cos(t) tr P and (c - b) = sin(t) tr P for a
+// symmetric P; so U = [[a + d, b - c], [c - b, a + d]] / |(a + d, c - b)|, with 1 as the
+// third diagonal entry.  Otherwise polar3's scaled Newton iteration with each step's
+// divisions taken through one reciprocal (this part's f64 divisions are slow); both agree
+// with polar3 to rounding, and this form's sums are not in the oracle's order anyway.
+__device__ void polar3_fp32form(const double* A, double* X) {
+    const bool flat = A[2] == 0.0 && A[5] == 0.0 && A[6] == 0.0 && A[7] == 0.0 && A[8] == 0.0;
+    if (flat) {
+        const double det2 = A[0] * A[4] - A[1] * A[3];
+        const double u = A[0] + A[4], v = A[3] - A[1];
+        const double nrm = sqrt(u * u + v * v);
+        if (det2 > 0.0 && nrm > 0.0 && isfinite(nrm)) {
+            const double r = 1.0 / nrm;
+            X[0] = u * r; X[1] = -v * r; X[2] = 0.0;
+            X[3] = v * r; X[4] = u * r;  X[5] = 0.0;
+            X[6] = 0.0;   X[7] = 0.0;    X[8] = 1.0;
+            return;
+        }
+    }
+    for (int q = 0; q < 9; ++q) X[q] = A[q];
+    if (flat) X[8] = 1.0;
+    for (int it = 0; it < 60; ++it) {
+        double cf[9];
+        cf[0] = X[4] * X[8] - X[5] * X[7];
+        cf[1] = X[5] * X[6] - X[3] * X[8];
+        cf[2] = X[3] * X[7] - X[4] * X[6];
+        cf[3] = X[2] * X[7] - X[1] * X[8];
+        cf[4] = X[0] * X[8] - X[2] * X[6];
+        cf[5] = X[1] * X[6] - X[0] * X[7];
+        cf[6] = X[1] * X[5] - X[2] * X[4];
+        cf[7] = X[2] * X[3] - X[0] * X[5];
+        cf[8] = X[0] * X[4] - X[1] * X[3];
+        const double det = (X[0] * cf[0] + X[1] * cf[1]) + X[2] * cf[2];
+        if (det == 0.0 || !isfinite(det)) {
+            for (int q = 0; q < 9; ++q) X[q] = (q % 4 == 0) ? 1.0 : 0.0;
+            return;
+        }
+        const double rdet = 1.0 / det;
+        double fx = 0.0, fy = 0.0, y[9];
+        for (int q = 0; q < 9; ++q) {
+            y[q] = cf[q] * rdet;
+            fx += X[q] * X[q];
+            fy += y[q] * y[q];
+        }
+        const double gm = sqrt(sqrt(fy / fx));
+        const double rgm = 1.0 / gm;
+        double ch = 0.0;
+        for (int q = 0; q < 9; ++q) {
+            const double xn = 0.5 * (gm * X[q] + y[q] * rgm);
+            const double d = xn - X[q];
+            ch += d * d;
+            X[q] = xn;
+        }
+        if (ch <= 1e-28) break;
+    }
+}
+
+// One block per object: the chunk partials added (strided shares, then the tree); PASS 0
+// writes the centre of mass, PASS 1 the rotation.
+template <int PASS>
+__global__ void __launch_bounds__(kRigidBlock) k_rigid_reduce32(const int* __restrict__ off, int chunks,
+                                                               const double* __restrict__ part,
+                                                               double* __restrict__ cm, double* __restrict__ rot) {
+    __shared__ double red[9][kRigidBlock];
+    const int o = blockIdx.x;
+    const int nc = (off[o + 1] - off[o] + kRigidChunk - 1) / kRigidChunk;
+    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int c = threadIdx.x; c < nc; c += kRigidBlock)
+        for (int e = 0; e < 9; ++e) v[e] += part[((size_t)o * chunks + c) * 9 + e];
+    block_sum_fixed<9>(v, red);
+    if (threadIdx.x != 0) return;
+    if (PASS == 0) {
+        for (int d = 0; d < 3; ++d) cm[3 * o + d] = red[d][0] / red[3][0];
+    } else {
+        double A[9], R[9];
+        for (int e = 0; e < 9; ++e) A[e] = red[e][0];
+        polar3_fp32form(A, R);
         bool small = true;
         for (int q = 0; q < 9; ++q) small = small && fabs(R[q]) < EPS;
         if (small)
             for (int q = 0; q < 9; ++q) R[q] = (q % 4 == 0) ? 1.0 : 0.0;
-        for (int d = 0; d < 3; ++d) cm_s[d] = cm[d];
-        for (int q = 0; q < 9; ++q) R_s[q] = R[q];
+        for (int q = 0; q < 9; ++q) rot[9 * o + q] = R[q];
     }
-    __syncthreads();
-    for (int q = threadIdx.x; q < m; q += blockDim.x) {
-        const int i = list[q];
+}
+
+__global__ void __launch_bounds__(kRigidBlock) k_rigid_move32(K32 k, P32 p, const int* __restrict__ off,
+                                                             const int* __restrict__ lists,
+                                                             const double* __restrict__ qtab,
+                                                             const double* __restrict__ cm,
+                                                             const double* __restrict__ rot) {
+    const int o = blockIdx.y;
+    const int m = off[o + 1] - off[o];
+    const int q0 = blockIdx.x * kRigidChunk;
+    const int q1 = min(m, q0 + kRigidChunk);
+    const double* R = rot + 9 * o;
+    const double* c = cm + 3 * o;
+    for (int q = q0 + threadIdx.x; q < q1; q += kRigidBlock) {
+        const int i = lists[off[o] + q];
         const double* qq = qtab + 3 * (size_t)p.ids[i].x;
         const float4 h = p.hi[i];
         float4 l = p.lo[i];
-        const double g0 = cm_s[0] + ((R_s[0] * qq[0] + R_s[1] * qq[1]) + R_s[2] * qq[2]);
-        const double g1 = cm_s[1] + ((R_s[3] * qq[0] + R_s[4] * qq[1]) + R_s[5] * qq[2]);
-        const double g2 = cm_s[2] + ((R_s[6] * qq[0] + R_s[7] * qq[1]) + R_s[8] * qq[2]);
+        const double g0 = c[0] + ((R[0] * qq[0] + R[1] * qq[1]) + R[2] * qq[2]);
+        const double g1 = c[1] + ((R[3] * qq[0] + R[4] * qq[1]) + R[5] * qq[2]);
+        const double g2 = c[2] + ((R[6] * qq[0] + R[7] * qq[1]) + R[8] * qq[2]);
         l.x = (float)((g0 - k.vs[0]) - (double)h.x);
         l.y = (float)((g1 - k.vs[1]) - (double)h.y);
         if (k.dim == 3) l.z = (float)((g2 - k.vs[2]) - (double)h.z);
@@ -670,24 +791,33 @@ __global__ void __launch_bounds__(1024) k_shape_match32(K32 k, P32 p, const int*
     }
 }
 
-// init_rigid_body (eng/solver_sph_base.py:467-470) from the uploaded f64 positions in upload
-// order: one thread per object sums its rest centre of mass, then every dynamic rigid
-// particle's rest offset x0 - rest cm is stored at its upload index (its id0).
-__global__ void k_rigid_rest32(int n, const int* __restrict__ ids_tab, const double* __restrict__ x,
-                               const double* __restrict__ mass, const int* __restrict__ mt,
-                               const int* __restrict__ oid, const int* __restrict__ dyn, double* __restrict__ q) {
-    if (threadIdx.x != 0) return;
+// init_rigid_body (eng/solver_sph_base.py:467-470) from the uploaded f64 positions, over the
+// object's list in upload order, one block per object (once, at upload): the rest centre of
+// mass (strided shares and the tree of block_sum_fixed), then every dynamic rigid particle's
+// rest offset x0 - rest cm stored at its upload index (its id0).
+__global__ void __launch_bounds__(kRigidBlock) k_rigid_rest32(const int* __restrict__ off,
+                                                             const int* __restrict__ lists,
+                                                             const double* __restrict__ x,
+                                                             const double* __restrict__ mass, double* __restrict__ q) {
+    __shared__ double red[4][kRigidBlock];
+    __shared__ double cm_s[3];
     const int o = blockIdx.x;
-    double cm[3] = {0.0, 0.0, 0.0}, sum_m = 0.0;
-    for (int i = 0; i < n; ++i) {
-        if (!(mt[i] == MAT_RIGID && dyn[i] && oid[i] == ids_tab[o])) continue;
-        for (int d = 0; d < 3; ++d) cm[d] += mass[i] * x[3 * (size_t)i + d];
-        sum_m += mass[i];
+    const int* list = lists + off[o];
+    const int m = off[o + 1] - off[o];
+    double v[4] = {0, 0, 0, 0};
+    for (int k = threadIdx.x; k < m; k += kRigidBlock) {
+        const int i = list[k];
+        for (int d = 0; d < 3; ++d) v[d] += mass[i] * x[3 * (size_t)i + d];
+        v[3] += mass[i];
     }
-    for (int d = 0; d < 3; ++d) cm[d] /= sum_m;
-    for (int i = 0; i < n; ++i)
-        if (mt[i] == MAT_RIGID && dyn[i] && oid[i] == ids_tab[o])
-            for (int d = 0; d < 3; ++d) q[3 * (size_t)i + d] = x[3 * (size_t)i + d] - cm[d];
+    block_sum_fixed<4>(v, red);
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; ++d) cm_s[d] = red[d][0] / red[3][0];
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += kRigidBlock) {
+        const int i = list[k];
+        for (int d = 0; d < 3; ++d) q[3 * (size_t)i + d] = x[3 * (size_t)i + d] - cm_s[d];
+    }
 }
 
 // WCSPH continuity + momentum (eng/solver_sph_wc.py:108-126).
@@ -1951,7 +2081,17 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
         if (!st->r_q) { fp32_destroy(st); return TSG_E_CUDA; }
         cudaMemcpyAsync(st->r_ids, rigid->ids.data(), sizeof(int) * rigid->ids.size(), cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(st->r_off, rigid->off.data(), sizeof(int) * rigid->off.size(), cudaMemcpyHostToDevice, s);
-        TSG_LAUNCH(k_rigid_rest32, st->rnobj, 32, s, n, st->r_ids, dx, d2, imt, ioid, idyn, st->r_q);
+        int maxm = 0;
+        for (size_t o = 0; o + 1 < rigid->off.size(); ++o) maxm = std::max(maxm, rigid->off[o + 1] - rigid->off[o]);
+        st->r_chunks = std::max(1, (maxm + kRigidChunk - 1) / kRigidChunk);
+        st->r_scratch = dal<int>(*st, rlist_scratch_ints(n, st->rnobj));
+        st->r_part = dal<double>(*st, 9 * (size_t)st->rnobj * st->r_chunks);
+        st->r_cm = dal<double>(*st, 3 * (size_t)st->rnobj);
+        st->r_rot = dal<double>(*st, 9 * (size_t)st->rnobj);
+        if (!st->r_scratch || !st->r_part || !st->r_cm || !st->r_rot) { fp32_destroy(st); return TSG_E_CUDA; }
+        build_rigid_lists(n, st->rnobj, RigidSlotUpload{imt, idyn, ioid, st->r_ids, st->rnobj}, st->r_scratch,
+                          st->r_off, st->r_list, s);
+        TSG_LAUNCH(k_rigid_rest32, st->rnobj, kRigidBlock, s, st->r_off, st->r_list, dx, d2, st->r_q);
     }
     TSG_LAUNCH(k_load32, nblk(n), TPB, s, k, dx, dv, d1, d2, d3, d4, imt, imid, ioid, idyn, islot, iscene, st->P[0]);
     if (soil && pp->stress) {  // (n, 3, 3) row-major -> six planes (upper triangle)
@@ -2475,7 +2615,15 @@ void f32::step_body(Fp32State& st, cudaStream_t s, bool collide, bool fold_disp)
 void fp32_solve_rigid(Fp32State& st, cudaStream_t s) {
     if (st.rnobj == 0) return;
     PhaseScope ph(s, PH_POS);
-    TSG_LAUNCH(k_shape_match32, st.rnobj, 1024, s, st.k, st.P[st.cur], st.r_ids, st.r_off, st.r_list, st.r_q);
+    const auto& p = st.P[st.cur];
+    build_rigid_lists(st.k.nd, st.rnobj, RigidSlot32{p.hi, p.ids, st.r_ids, st.rnobj}, st.r_scratch, st.r_off,
+                      st.r_list, s);
+    const dim3 g(st.r_chunks, st.rnobj);
+    TSG_LAUNCH(k_rigid_part32<0>, g, kRigidBlock, s, st.k, p, st.r_off, st.r_list, st.r_q, st.r_cm, st.r_part);
+    TSG_LAUNCH(k_rigid_reduce32<0>, st.rnobj, kRigidBlock, s, st.r_off, st.r_chunks, st.r_part, st.r_cm, st.r_rot);
+    TSG_LAUNCH(k_rigid_part32<1>, g, kRigidBlock, s, st.k, p, st.r_off, st.r_list, st.r_q, st.r_cm, st.r_part);
+    TSG_LAUNCH(k_rigid_reduce32<1>, st.rnobj, kRigidBlock, s, st.r_off, st.r_chunks, st.r_part, st.r_cm, st.r_rot);
+    TSG_LAUNCH(k_rigid_move32, g, kRigidBlock, s, st.k, p, st.r_off, st.r_list, st.r_q, st.r_cm, st.r_rot);
 }
 
 void fp32_step_body(Fp32State& st, bool collide, cudaStream_t s) { f32::step_body(st, s, collide); }

@@ -625,10 +625,12 @@ struct Fp32State {
     int *ovf_list = nullptr, *novf = nullptr;  // particles whose neighbours exceed the list capacity
     int *sact = nullptr, *nsact = nullptr;     // static-block particles with a non-empty list
     // dynamic rigid bodies (WCSPH): objects, per-object list slices, and each rigid
-    // particle's rest offset x0 - rest centre of mass in f64, indexed by id0
-    int rnobj = 0;
-    int *r_ids = nullptr, *r_off = nullptr, *r_list = nullptr;
-    double* r_q = nullptr;
+    // particle's rest offset x0 - rest centre of mass in f64, indexed by id0; the shape
+    // matching's per-chunk partial sums (rnobj x r_chunks x 9), centres of mass (3 rnobj)
+    // and rotations (9 rnobj)
+    int rnobj = 0, r_chunks = 0;
+    int *r_ids = nullptr, *r_off = nullptr, *r_list = nullptr, *r_scratch = nullptr;
+    double *r_q = nullptr, *r_part = nullptr, *r_cm = nullptr, *r_rot = nullptr;
     unsigned* maxdisp = nullptr;               // squared displacement since the last list build
     bool built = false;
     double* stage = nullptr;       // f64 export staging (9 n)

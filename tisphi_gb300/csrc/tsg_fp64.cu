@@ -26,6 +26,7 @@
 
 #include "tsg_internal.h"
 #include "tsg_polar.cuh"
+#include "tsg_rigid_list.cuh"
 
 namespace tsg {
 
@@ -1039,85 +1040,126 @@ __global__ void k_rigid_reaction(Consts c, Persist64 p, Trans64 t, const int* __
     for (int d = 0; d < 3; ++d) t.d_vel[(size_t)d * n + j] = dvj[d];
 }
 
+// Object slot of a dynamic rigid particle (-1 for any other), for the list builder.
+struct RigidSlot64 {
+    const int* mt;
+    const int* dyn;
+    const int* oid;
+    const int* ids;
+    int nobj;
+    __device__ int operator()(int i) const {
+        if (mt[i] != MAT_RIGID || !dyn[i]) return -1;
+        const int id = oid[i];
+        for (int o = 0; o < nobj; ++o)
+            if (ids[o] == id) return o;
+        return -1;
+    }
+};
+
+// The object sums of the shape matching are serial sums in ascending particle order (the
+// oracle's order, so that the results are bit-identical).  The block stages each chunk of
+// kSMChunk particles' terms (products rounded as in the serial expression: this unit is
+// compiled without contracted multiply-adds) in shared memory with all its threads, and
+// one thread adds them in order: the dependent additions run from shared memory instead of
+// behind one gather per particle.
+constexpr int kSMChunk = 512;
+
 // init_rigid_body / calc_rigid_rest_m (eng/solver_sph_base.py:467-470, :517-518): the rest
 // centre of mass of every dynamic rigid object from the uploaded positions, summed in upload
-// order by one thread per object (before the first sort).
-__global__ void k_rest_cm(Consts c, Persist64 p, Rigid64 rb) {
+// order (the object's list, built before the first sort), one block per object.
+__global__ void __launch_bounds__(kSMChunk) k_rest_cm(Consts c, Persist64 p, Rigid64 rb) {
+    __shared__ double buf[4][kSMChunk];
     const int o = blockIdx.x;
-    if (threadIdx.x != 0) return;
-    const int oid = rb.obj_id[o];
+    const int* list = rb.list + rb.off[o];
+    const int m = rb.off[o + 1] - rb.off[o];
     const int n = c.n;
     double cm[3] = {0.0, 0.0, 0.0}, sum_m = 0.0;
-    for (int i = 0; i < n; ++i) {
-        if (!(p.mat_type[i] == MAT_RIGID && p.is_dynamic[i] && p.obj_id[i] == oid)) continue;
-        const double mi = p.mass[i];
-        for (int d = 0; d < 3; ++d) cm[d] = cm[d] + mi * p.x[(size_t)d * n + i];
-        sum_m += mi;
-    }
-    for (int d = 0; d < 3; ++d) rb.rest_cm[3 * o + d] = cm[d] / sum_m;
-}
-
-// solve_constraints (eng/solver_sph_base.py:478-500), one block per dynamic rigid object:
-// the object's particles listed in ascending order (block-wide ballot compaction), then by
-// one thread in that order the centre of mass (calc_cm, :502-511) and
-// A = sum (m_V rho p) q^T (p = x - cm, q = x0 - rest cm), R = polar(A) (identity when every
-// entry is below 1e-8), and finally every particle x += (cm + R q) - x.
-__global__ void __launch_bounds__(1024) k_shape_match(Consts c, Persist64 p, Rigid64 rb) {
-    const int o = blockIdx.x;
-    const int oid = rb.obj_id[o];
-    int* list = rb.list + rb.off[o];
-    __shared__ int warp_tot[32];
-    __shared__ int base_s;
-    __shared__ double cm_s[3], R_s[9];
-    const int n = c.n;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (threadIdx.x == 0) base_s = 0;
-    __syncthreads();
-    for (int i0 = 0; i0 < n; i0 += blockDim.x) {
-        const int i = i0 + threadIdx.x;
-        const bool on = i < n && p.mat_type[i] == MAT_RIGID && p.is_dynamic[i] && p.obj_id[i] == oid;
-        const unsigned bal = __ballot_sync(0xffffffffu, on);
-        if (lane == 0) warp_tot[wid] = __popc(bal);
-        __syncthreads();
-        int before = 0, total = 0;
-        for (int w = 0; w < nw; ++w) {
-            if (w < wid) before += warp_tot[w];
-            total += warp_tot[w];
-        }
-        if (on) list[base_s + before + __popc(bal & ((1u << lane) - 1u))] = i;
-        __syncthreads();
-        if (threadIdx.x == 0) base_s += total;
-        __syncthreads();
-    }
-    const int m = base_s;
-    if (threadIdx.x == 0) {
-        double cm[3] = {0.0, 0.0, 0.0}, sum_m = 0.0;
-        for (int k = 0; k < m; ++k) {
+    for (int k0 = 0; k0 < m; k0 += kSMChunk) {
+        const int k = k0 + threadIdx.x;
+        if (k < m) {
             const int i = list[k];
             const double mi = p.mass[i];
-            for (int d = 0; d < 3; ++d) cm[d] = cm[d] + mi * p.x[(size_t)d * n + i];
-            sum_m += mi;
+            for (int d = 0; d < 3; ++d) buf[d][threadIdx.x] = mi * p.x[(size_t)d * n + i];
+            buf[3][threadIdx.x] = mi;
         }
-        for (int d = 0; d < 3; ++d) cm[d] = cm[d] / sum_m;
-        double A[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int k = 0; k < m; ++k) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int cnt = min(kSMChunk, m - k0);
+            for (int q = 0; q < cnt; ++q) {
+                for (int d = 0; d < 3; ++d) cm[d] = cm[d] + buf[d][q];
+                sum_m += buf[3][q];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; ++d) rb.rest_cm[3 * o + d] = cm[d] / sum_m;
+}
+
+// solve_constraints (eng/solver_sph_base.py:478-500), one block per dynamic rigid object,
+// over its list (ascending particle order, rebuilt after every sort): the centre of mass
+// (calc_cm, :502-511) and A = sum (m_V rho p) q^T (p = x - cm, q = x0 - rest cm), both
+// summed in list order, R = polar(A) (identity when every entry is below 1e-8), and finally
+// every particle x += (cm + R q) - x.
+__global__ void __launch_bounds__(kSMChunk) k_shape_match(Consts c, Persist64 p, Rigid64 rb) {
+    __shared__ double buf[9][kSMChunk];
+    __shared__ double cm_s[3], R_s[9];
+    const int o = blockIdx.x;
+    const int* list = rb.list + rb.off[o];
+    const int m = rb.off[o + 1] - rb.off[o];
+    const int n = c.n;
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double sum_m = 0.0;
+    for (int k0 = 0; k0 < m; k0 += kSMChunk) {
+        const int k = k0 + threadIdx.x;
+        if (k < m) {
+            const int i = list[k];
+            const double mi = p.mass[i];
+            for (int d = 0; d < 3; ++d) buf[d][threadIdx.x] = mi * p.x[(size_t)d * n + i];
+            buf[3][threadIdx.x] = mi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int cnt = min(kSMChunk, m - k0);
+            for (int q = 0; q < cnt; ++q) {
+                for (int d = 0; d < 3; ++d) acc[d] = acc[d] + buf[d][q];
+                sum_m += buf[3][q];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; ++d) cm_s[d] = acc[d] / sum_m;
+    __syncthreads();
+    for (int q = 0; q < 9; ++q) acc[q] = 0.0;
+    for (int k0 = 0; k0 < m; k0 += kSMChunk) {
+        const int k = k0 + threadIdx.x;
+        if (k < m) {
             const int i = list[k];
             const double sc = p.m_V[i] * p.density[i];
             double sp[3], q[3];
             for (int d = 0; d < 3; ++d) {
                 q[d] = p.x0[(size_t)d * n + i] - rb.rest_cm[3 * o + d];
-                sp[d] = sc * (p.x[(size_t)d * n + i] - cm[d]);
+                sp[d] = sc * (p.x[(size_t)d * n + i] - cm_s[d]);
             }
             for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) A[3 * a + b] = A[3 * a + b] + sp[a] * q[b];
+                for (int b = 0; b < 3; ++b) buf[3 * a + b][threadIdx.x] = sp[a] * q[b];
         }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int cnt = min(kSMChunk, m - k0);
+            for (int q = 0; q < cnt; ++q)
+                for (int e = 0; e < 9; ++e) acc[e] = acc[e] + buf[e][q];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
         double R[9];
-        polar3(A, R);
+        polar3(acc, R);
         bool small = true;
         for (int q = 0; q < 9; ++q) small = small && fabs(R[q]) < EPS;
         if (small)
             for (int q = 0; q < 9; ++q) R[q] = (q % 4 == 0) ? 1.0 : 0.0;
-        for (int d = 0; d < 3; ++d) cm_s[d] = cm[d];
         for (int q = 0; q < 9; ++q) R_s[q] = R[q];
     }
     __syncthreads();
@@ -1135,6 +1177,11 @@ __global__ void __launch_bounds__(1024) k_shape_match(Consts c, Persist64 p, Rig
     }
 }
 
+static void rigid_lists64(const Consts& c, const Persist64& p, const Rigid64& r, cudaStream_t s) {
+    build_rigid_lists(c.n, r.nobj, RigidSlot64{p.mat_type, p.is_dynamic, p.obj_id, r.obj_id, r.nobj}, r.scratch,
+                      r.off, r.list, s);
+}
+
 #define DISPATCH_DIM(c, KERNEL, GRID, ...)                                   \
     do {                                                                     \
         if ((c).dim == 2) TSG_LAUNCH(KERNEL<2>, GRID, TPB, s, __VA_ARGS__);       \
@@ -1147,13 +1194,16 @@ void fp64_kernel_corr(const Consts& c, const Persist64& p, Trans64& t, const Gri
 }
 
 void fp64_rest_cm(const Consts& c, const Persist64& p, const Rigid64& r, cudaStream_t s) {
-    if (r.nobj > 0) TSG_LAUNCH(k_rest_cm, r.nobj, 32, s, c, p, r);
+    if (r.nobj <= 0) return;
+    rigid_lists64(c, p, r, s);
+    TSG_LAUNCH(k_rest_cm, r.nobj, kSMChunk, s, c, p, r);
 }
 
 void fp64_solve_rigid(const Consts& c, Persist64& p, const Rigid64& r, cudaStream_t s) {
     if (r.nobj <= 0) return;
     PhaseScope ph(s, PH_POS);
-    TSG_LAUNCH(k_shape_match, r.nobj, 1024, s, c, p, r);
+    rigid_lists64(c, p, r, s);
+    TSG_LAUNCH(k_shape_match, r.nobj, kSMChunk, s, c, p, r);
 }
 
 void fp64_density_sum(const Consts& c, const Persist64& p, const Trans64& t, const Grid& g, double* out,

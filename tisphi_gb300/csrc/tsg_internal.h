@@ -58,13 +58,20 @@ struct Consts {
 
 // Dynamic rigid bodies (eng/solver_sph_base.py:467-518): object ids, rest centres of mass
 // (from the uploaded positions, in upload order) and, per object, the slice of `list`
-// that the shape-matching kernel fills with the object's particles in ascending order.
+// that the list builder (tsg_rigid_list.cuh) fills with the object's particles in
+// ascending order before every shape matching.
+// Block size of the rigid-object list builder (tsg_rigid_list.cuh) and its scratch size.
+constexpr int kRListBlock = 256;
+inline int rlist_blocks(int n) { return (n + kRListBlock - 1) / kRListBlock; }
+inline size_t rlist_scratch_ints(int n, int nobj) { return (size_t)nobj * (size_t)rlist_blocks(n); }
+
 struct Rigid64 {
     int nobj = 0;
     int* obj_id = nullptr;      // nobj (device)
     double* rest_cm = nullptr;  // 3 nobj (device)
     int* off = nullptr;         // nobj + 1 (device): slice starts in list
     int* list = nullptr;        // n_rigid_dyn (device)
+    int* scratch = nullptr;     // nobj * ceil(n / 256) (device): the list builder's block offsets
 };
 
 // Persistent per-particle fields (permuted by the sort; double-buffered).
