@@ -877,6 +877,105 @@ def run_column(args):
     print(json.dumps(line))
 
 
+def run_kernels(args):
+    """Every kernel family of both forms at least once, at sizes above the 129 MB L2 where the
+    scene allows: the command that the per-kernel DRAM / cache survey captures (one line of
+    wall times per leg, no bench figure).  Each leg builds its scene in both forms, steps it
+    three times and frees it; the particle-system extras (density summation, field export,
+    the visual buffer, the allocation-free sort) run on the legs that name them, the
+    ensemble and both adjoints on small scenes of their stated kind."""
+    import ctypes
+
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    from tisphi_gb300 import _native as nat
+    from tisphi_gb300 import build_native, scenes
+    build_native.build()
+    from tisphi_gb300.adjoint import MuIRollout, WCRollout, distal_loss
+    from tisphi_gb300.batch import SceneBatch
+    from tisphi_gb300.configer_builder import SimConfiger
+    from tisphi_gb300.simulation import Simulation
+    lib = nat.load()
+    # eager launches (the phase timer's mode) rather than graph replays, so that a
+    # per-launch profiler sees every kernel of the step sequences
+    lib.tsg_profile(1)
+
+    def with_boundary(d, b):
+        d["Configuration"]["boundary"] = b
+        return d
+
+    col = dict(spacing=0.0005, width=1.0, height=0.5, domain=(2.5, 0.6))
+    legs = [
+        ("3D WCSPH dambreak, spacing 0.0075 m, LF, CSPM", scenes.dambreak_3d(spacing=0.0075),
+         {"density", "export", "visual"}),
+        ("2D WCSPH dambreak, spacing 0.001 m, RK4, XSPH, CSPM",
+         scenes.dambreak_2d(spacing=0.001, integration=4, xsph=True, corr=1), {"density"}),
+        ("2D WCSPH dambreak, spacing 0.001 m, SE, cubic spline, dummy + repulsive boundary",
+         with_boundary(scenes.dambreak_2d(spacing=0.001, integration=1, kernel=0), 4), set()),
+        ("2D mu(I) column 1.0 x 0.5 m, spacing 0.0005 m, SE, CSPM",
+         scenes.column_2d(method=2, integration=1, corr=1, **col), {"export"}),
+        ("2D Drucker-Prager column 1.0 x 0.5 m, spacing 0.0005 m, LF, XSPH",
+         scenes.column_2d(method=3, integration=2, xsph=True, **col), set()),
+        # small enough for the allocation-free sort's fixed arrays (262,144 particles and cells)
+        ("2D water with a dynamic rigid box, spacing 0.002 m, LF", scenes.floating_box_2d(spacing=0.002),
+         {"noalloc"}),
+    ]
+    out = []
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for name, d, extras in legs:
+        for precision in ("fp32_mixed", "fp64"):
+            t0 = time.perf_counter()
+            sim = Simulation(SimConfiger(config=d), precision=precision)
+            sim.solver.step(3)
+            ps = sim.ps
+            if "density" in extras:
+                sim.solver.calc_density()
+            if "export" in extras:
+                host = [torch.empty((ps.particle_max_num, 3), dtype=torch.float64).pin_memory() for _ in range(2)]
+                ps.read_fields(("x", "v"), host)
+            if "visual" in extras:
+                ps.visual()
+            if "noalloc" in extras and precision == "fp32_mixed":
+                n, G = ps.particle_max_num, ps.grid_num_total
+                cs = torch.empty(G + 2, dtype=torch.int32, device="cuda")
+                perm = torch.empty(n, dtype=torch.int32, device="cuda")
+                x = ps.field("x").contiguous()
+                nat.check(lib.tsg_sort_noalloc(ctypes.byref(ps._cfg), ctypes.c_void_p(x.data_ptr()), n,
+                                               ctypes.c_void_p(cs.data_ptr()), ctypes.c_void_p(perm.data_ptr()),
+                                               stream), "tsg_sort_noalloc")
+            torch.cuda.synchronize()
+            out.append({"leg": name, "form": precision, "n_particles": ps.particle_max_num,
+                        "seconds": time.perf_counter() - t0})
+            del sim, ps
+    t0 = time.perf_counter()
+    batch = SceneBatch(scenes.dambreak_ensemble(64))
+    batch.step(3)
+    torch.cuda.synchronize()
+    out.append({"leg": "64-scene 2D WCSPH ensemble, LF", "form": "fp32_mixed", "n_particles": batch.n,
+                "seconds": time.perf_counter() - t0})
+    del batch
+    for name, model, params, target in (
+            ("mu(I) column adjoint, spacing 0.002 m, 10 SE steps",
+             MuIRollout(scenes.column_2d(method=2, spacing=0.002, dt=2e-5), nsteps=10, checkpoint_every=5),
+             [21.9, 0.0], 0.35),
+            ("WCSPH dambreak adjoint, spacing 0.01 m, 10 SE steps",
+             WCRollout(scenes.dambreak_2d(spacing=0.01, width=0.6, height=0.4, domain=(1.2, 0.8), integration=1),
+                       nsteps=10, checkpoint_every=5), None, 0.7)):
+        t0 = time.perf_counter()
+        p = torch.tensor(params if params else [model.stiffness, model.viscosity], dtype=torch.float64,
+                         requires_grad=True)
+        distal_loss(model(p), target=target)[0].backward()
+        torch.cuda.synchronize()
+        out.append({"leg": name, "form": "fp32_mixed", "n_particles": model.n, "seconds": time.perf_counter() - t0})
+        del model
+    nph = len(nat.PHASES)
+    lib.tsg_profile_read((ctypes.c_double * nph)(), (ctypes.c_int64 * nph)(), nph)
+    lib.tsg_profile(0)
+    print(json.dumps({"workload": "kernel survey (every kernel family, both forms)", "legs": out,
+                      "data": "synthetic"}))
+
+
 def run_reference(args):
     rank, ws, dist = dist_init(args)
     if rank != 0:
@@ -926,7 +1025,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["both", "fp32_mixed", "fp64"], default="both")
-    ap.add_argument("--workload", choices=["3d", "2d", "batch", "adjoint", "rollout", "column"], default="3d")
+    ap.add_argument("--workload", choices=["3d", "2d", "batch", "adjoint", "rollout", "column", "kernels"], default="3d")
     ap.add_argument("--column-steps", type=int, default=6100, help="run length for --workload column")
     ap.add_argument("--adjoint-steps", type=int, default=2000, help="rollout length for --workload adjoint")
     ap.add_argument("--scenes", type=int, default=256, help="ensemble size for --workload batch")
@@ -954,6 +1053,8 @@ def main():
         run_rollout(args)
     elif args.workload == "column":
         run_column(args)
+    elif args.workload == "kernels":
+        run_kernels(args)
     else:
         run_ours(args)
 
