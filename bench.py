@@ -19,6 +19,12 @@ host cores for a bounded sample of the same workload.
 
 ``--impl reference`` times the reference algorithm's CPU restatement (the oracle) instead,
 on all host cores, and prints the reference-arm line.
+
+Other workloads (``--workload``): ``batch`` (the 256-scene ensemble, batched against scene
+by scene), ``adjoint`` (the differentiable column's gradients against finite differences),
+``rollout`` (2,000 steps of the 3D dambreak in both forms), ``column`` (the granular column
+at its stated size), ``kernels`` (every kernel family of both forms once, the command of
+the per-kernel profiler survey).
 """
 import argparse
 import json

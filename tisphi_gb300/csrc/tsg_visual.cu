@@ -67,32 +67,44 @@ __device__ double value_of(const VisFields& f, int title, int i) {
     }
 }
 
-__device__ __forceinline__ void atomic_minmax(double* mm, double v) {
+// mm[0] = max(mm[0], vmax), mm[1] = min(mm[1], vmin) (a value that compares false, NaN, is
+// never stored).
+__device__ __forceinline__ void atomic_minmax(double* mm, double vmax, double vmin) {
     unsigned long long* amax = reinterpret_cast<unsigned long long*>(mm);
     unsigned long long* amin = reinterpret_cast<unsigned long long*>(mm + 1);
     unsigned long long old = *amax;
-    while (__longlong_as_double(old) < v) {
-        unsigned long long prev = atomicCAS(amax, old, __double_as_longlong(v));
+    while (__longlong_as_double(old) < vmax) {
+        unsigned long long prev = atomicCAS(amax, old, __double_as_longlong(vmax));
         if (prev == old) break;
         old = prev;
     }
     old = *amin;
-    while (__longlong_as_double(old) > v) {
-        unsigned long long prev = atomicCAS(amin, old, __double_as_longlong(v));
+    while (__longlong_as_double(old) > vmin) {
+        unsigned long long prev = atomicCAS(amin, old, __double_as_longlong(vmin));
         if (prev == old) break;
         old = prev;
     }
 }
 
-// Values of the selected particles (real ones, and dummies when shown); range over flow.
+// Values of the selected particles (real ones, and dummies when shown); range over flow:
+// reduced over the warp first (max and min are exact in any order), then one update of the
+// range per warp.
 __global__ void k_vis_value(VisFields f, int title, int show_bdy, double* __restrict__ val, double* mm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= f.n) return;
-    const int t = f.mat_type[i];
-    if (!(real_p(t) || (show_bdy && t == MAT_DUMMY))) return;
-    const double v = value_of(f, title, i);
-    val[i] = v;
-    if (flow_p(t)) atomic_minmax(mm, v);
+    double hi = -INFINITY, lo = INFINITY;
+    if (i < f.n) {
+        const int t = f.mat_type[i];
+        if (real_p(t) || (show_bdy && t == MAT_DUMMY)) {
+            const double v = value_of(f, title, i);
+            val[i] = v;
+            if (flow_p(t)) hi = lo = v;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        hi = fmax(hi, __shfl_down_sync(0xffffffffu, hi, o));
+        lo = fmin(lo, __shfl_down_sync(0xffffffffu, lo, o));
+    }
+    if ((threadIdx.x & 31) == 0 && lo <= hi) atomic_minmax(mm, hi, lo);
 }
 
 // The given / fixed bounds of v_maxmin (one thread).
