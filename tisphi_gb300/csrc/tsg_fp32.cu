@@ -1143,24 +1143,48 @@ __global__ void k_post_mui32(K32 k, P32 p, T32 t) {
 }
 
 // mu(I) stress regularisation (eng/solver_sph_muI.py:151-156): stress_i = CSPM_f_i
-// sum_{soil j} m_Vj stress_tmp_j W_ij at the moved positions, by direct enumeration over
-// the cell table of the last sort (every soil particle; the prefilter positions predate
-// this step's move, so it is off).  Both phases of the reference's racy in-place update
-// are separated: every read is of stress_tmp.
+// sum_{soil j} m_Vj stress_tmp_j W_ij at the moved positions.  Both phases of the reference's
+// racy in-place update are separated: every read is of stress_tmp.  The neighbours come
+// from i's list while the lists still hold every pair within the support at the moved
+// positions - no particle has moved more than 0.49 skin since the build (*maxd, measured
+// from the moved positions just before this pass, against list_d2 > 0; a pair within R now
+// was then within R + 0.98 skin at the build) and i's list did not overflow - and
+// otherwise by direct enumeration over the cell table of the last sort (prefilter off: its
+// positions predate the move).  The list builder enumerates the same stencil in the same
+// order and the list offsets give the same displacement bits, so both visit the soil
+// neighbours within the support in the same order and give the same sums (for particles
+// that have not changed cell since the sort; otherwise the order, not the set, differs).
 template <int DIM>
 __global__ void k_reg_mui32(K32 k, P32 p, T32 t, const float4* __restrict__ PF, const int* __restrict__ dstart,
-                            const int* __restrict__ sstart) {
+                            const int* __restrict__ sstart, const unsigned* __restrict__ maxd, float list_d2) {
+    const bool lists_ok = list_d2 > 0.f && __uint_as_float(*maxd) <= list_d2;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.nd; i += gridDim.x * blockDim.x) {
         if (tf_type(p.hi[i].w) != MAT_SOIL) continue;
         const size_t n = k.n;
         float s[6] = {0, 0, 0, 0, 0, 0};
-        enum_neighbors<DIM>(k, i, p.hi, p.lo, PF, dstart, sstart, false, [&](int j, const float*, float r2) {
-            if (tf_type(p.hi[j].w) != MAT_SOIL) return;
-            const float mw = p.lo[j].w * w_val(k, fast_sqrt(r2));
-            for (int q = 0; q < 6; ++q) s[q] += mw * t.sigt[q * n + j];
-        }, false, false);
+        const int m = t.cnt[i];
+        if (lists_ok && m <= k.maxn) {
+            const float4 lo_i = p.lo[i];
+            for (int q = 0; q < m; ++q) {
+                const int e = t.nbr[(size_t)q * n + i];
+                if (class_type((e >> kEntryBits) & 7) != MAT_SOIL) continue;
+                const int j = e & kEntryMask;
+                const float4 l = p.lo[j];
+                float d[3];
+                const float r2 = list_delta<DIM>(k, e, lo_i, l, d);
+                if (!(r2 < k.R2)) continue;
+                const float mw = l.w * w_val(k, fast_sqrt(r2));
+                for (int c = 0; c < 6; ++c) s[c] += mw * t.sigt[c * n + j];
+            }
+        } else {
+            enum_neighbors<DIM>(k, i, p.hi, p.lo, PF, dstart, sstart, false, [&](int j, const float*, float r2) {
+                if (tf_type(p.hi[j].w) != MAT_SOIL) return;
+                const float mw = p.lo[j].w * w_val(k, fast_sqrt(r2));
+                for (int c = 0; c < 6; ++c) s[c] += mw * t.sigt[c * n + j];
+            }, false, false);
+        }
         const float f = t.cf[i];
-        for (int q = 0; q < 6; ++q) p.sig[q * n + i] = s[q] * f;
+        for (int c = 0; c < 6; ++c) p.sig[c * n + i] = s[c] * f;
     }
 }
 
@@ -2528,8 +2552,20 @@ void fp32_advect(Fp32State& st, int which, cudaStream_t s) {
         if (k.solver == 1) TSG_LAUNCH(k_post_wc32, nblk(k.nd), TPB, s, k, p);
         else if (k.solver == 2) {
             TSG_LAUNCH(k_post_mui32, nblk(k.nd), TPB, s, k, p, st.T);
-            if (k.dim == 2) TSG_LAUNCH(k_reg_mui32<2>, nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart);
-            else TSG_LAUNCH(k_reg_mui32<3>, nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart);
+            // the regularisation reads the lists while no particle has moved more than 0.49
+            // skin since their build ((0.49 / 0.45)^2 = 1.1857 times the rebuild threshold),
+            // measured here from the moved positions (the next step's check finds the same)
+            float list_d2 = -1.f;
+            if (st.lists_valid && k.disp2_limit > 0.f) {
+                TSG_LAUNCH(k_disp32, nblk(k.nd), TPB, s, k, p.hi, p.lo, st.pf, st.maxdisp);
+                list_d2 = k.disp2_limit * 1.185f;
+            }
+            if (k.dim == 2)
+                TSG_LAUNCH(k_reg_mui32<2>, nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.maxdisp,
+                           list_d2);
+            else
+                TSG_LAUNCH(k_reg_mui32<3>, nblk(k.nd), TPB, s, k, p, st.T, st.pf, st.dstart, st.sstart, st.maxdisp,
+                           list_d2);
         } else TSG_LAUNCH(k_post_dp32, nblk(k.nd), TPB, s, k, p, st.T);
         break;
     }
