@@ -7,8 +7,8 @@ that scatter, and replace ti.polar_decompose by the same scaled Newton iteration
 form is bit-identical to the oracle (the golden fixture wc2d_rigid pins the oracle to the
 reference's own rigid-body code run under the Taichi emulator).  Cases: a 2D water column
 with a floating box (leap-frog over 300 steps, symplectic Euler + XSPH), a sinking box, the
-3D counterpart with CSPM (also with the box given as a mesh body), and a mu(I) column with a
-box resting on the sand.  The FP32-mixed
+3D counterpart with CSPM (also with the box given as a mesh body), two bodies of 1,200 and
+300 particles on one water column, and a mu(I) column with a box resting on the sand.  The FP32-mixed
 WCSPH form takes them too (reaction gathered over each rigid particle's list, shape matching
 in f64 on its hi + lo positions), within its tolerances against the oracle; granular scenes
 with dynamic rigid bodies take the FP64 form.
@@ -47,6 +47,20 @@ def _box_on_sand():
     return d
 
 
+def _two_boxes():
+    """Two dynamic bodies thrown onto a 2D water column: a 1,200-particle box (more than one
+    chunk of the FP32-mixed form's object sums, three of the FP64 form's staged sums) and a
+    300-particle denser one, so that the object lists, slices and per-object sums serve two
+    objects."""
+    from tisphi_gb300 import scenes
+    d = scenes.floating_box_2d(spacing=0.004, dt=2e-5, jitter=4e-5, box=(0.16, 0.12), box_at=(0.1, 0.4))
+    d["Blocks"][-1]["velocity"] = [0.5, -3.0, 0.0]
+    d["Materials"].append({"matId": 2, "matType": 11, "color": [55, 155, 55], "density0": 2000.0})
+    d["Blocks"].append({"objectId": 2, "size": [0.08, 0.06, 0.05], "translation": [0.4, 0.4, 0.0],
+                        "velocity": [-0.5, -3.0, 0.0], "materialId": 2, "isDynamic": True})
+    return d
+
+
 def _cases():
     from tisphi_gb300 import scenes
     return {
@@ -57,6 +71,7 @@ def _cases():
         "mui_box_on_sand": (_box_on_sand(), 100),
         # the box as a mesh body (a unit-box OBJ voxelised at the particle diameter)
         "3d_mesh_body": (mesh_box_scene_3d(write_box_obj(os.path.join(_OBJ_DIR, "unit_box.obj"))), 20),
+        "2d_two_boxes": (_two_boxes(), 100),
     }
 
 
@@ -71,14 +86,17 @@ def test_rigid_fp64_bit_exact(oracle_lib, native, name):
     sim.solver.step(steps)
     orc.step(steps)
     _compare(sim, orc, FIELDS, f"{name} after {steps} steps")
-    # the body moved and kept its shape: pairwise distances of its particles unchanged
+    # every body moved and kept its shape: pairwise distances of its particles unchanged
     mt = orc.get("mat_type")
     xr = orc.get("x")[mt == 11]
     x0 = orc.scene.x[orc.get("id0")[mt == 11].astype(np.int64)]
-    assert np.max(np.abs(xr - x0)) > 1e-6
-    d0 = np.linalg.norm(x0[:, None, :] - x0[None, :, :], axis=-1)
-    d1 = np.linalg.norm(xr[:, None, :] - xr[None, :, :], axis=-1)
-    assert np.max(np.abs(d1 - d0)) < 1e-9
+    obj = orc.get("obj_id")[mt == 11]
+    for o in np.unique(obj):
+        sel = obj == o
+        assert np.max(np.abs(xr[sel] - x0[sel])) > 1e-6
+        d0 = np.linalg.norm(x0[sel][:, None, :] - x0[sel][None, :, :], axis=-1)
+        d1 = np.linalg.norm(xr[sel][:, None, :] - xr[sel][None, :, :], axis=-1)
+        assert np.max(np.abs(d1 - d0)) < 1e-9, f"body {o}"
 
 
 def test_rigid_stage_calls_match_step(native):
@@ -110,7 +128,7 @@ def _by_id(ps_ids, v):
     return out
 
 
-@pytest.mark.parametrize("name", ["2d_lf_float", "2d_sink", "3d_cspm", "3d_mesh_body"])
+@pytest.mark.parametrize("name", ["2d_lf_float", "2d_sink", "3d_cspm", "3d_mesh_body", "2d_two_boxes"])
 def test_rigid_fp32_mixed_close(oracle_lib, native, name):
     """The FP32-mixed WCSPH form with dynamic rigid bodies against the oracle: fluid density
     within 1e-5 relative, every position within 2e-6 m, the rigid particles' accelerations
