@@ -296,7 +296,9 @@ __device__ __forceinline__ float list_delta(const K32& k, int e, const float4& l
 // neighbour's payload, loaded together with its lo record (before the support test, so the
 // two gathers overlap; the list's skin pairs load it for nothing).  Two neighbours per trip;
 // the next trip's two list entries are loaded before this trip's gathers, so the entry
-// stream (from DRAM) overlaps the gathers and the maths.
+// stream (from DRAM) overlaps the gathers and the maths.  Entries are read once, with the
+// evict-first streaming hint (ld.global.cs), so that they do not push the neighbours'
+// records out of L1 and L2.
 // REC: the payload is the neighbour's v_tmp record, loaded together with its lo record in
 // one 256-bit read (ldg_rec) instead of through gather(j) (the overflow traversal still
 // calls gather).
@@ -319,10 +321,10 @@ __device__ __forceinline__ void for_nbrs_g(const K32& k, int i, const int* __res
         };
         int s = 0;
         int e0 = 0, e1 = 0;
-        if (m > 1) { e0 = lp[0]; e1 = lp[stride]; lp += 2 * stride; }
+        if (m > 1) { e0 = __ldcs(lp); e1 = __ldcs(lp + stride); lp += 2 * stride; }
         for (; s + 1 < m; s += 2) {
             int n0 = 0, n1 = 0;
-            if (s + 3 < m) { n0 = lp[0]; n1 = lp[stride]; lp += 2 * stride; }
+            if (s + 3 < m) { n0 = __ldcs(lp); n1 = __ldcs(lp + stride); lp += 2 * stride; }
             const int j0 = e0 & kEntryMask, j1 = e1 & kEntryMask;
             float4 l0, l1;
             decltype(gather(0)) g0, g1;
@@ -380,11 +382,11 @@ __device__ __forceinline__ void for_list4(const K32& k, int i, const int* __rest
     const int* lp = nbr + i;
     int e[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) e[u] = u < m ? lp[(size_t)u * stride] : 0;
+    for (int u = 0; u < 4; ++u) e[u] = u < m ? __ldcs(lp + (size_t)u * stride) : 0;
     for (int s = 0; s < m; s += 4) {
         int nx[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) nx[u] = s + 4 + u < m ? lp[(size_t)(s + 4 + u) * stride] : 0;
+        for (int u = 0; u < 4; ++u) nx[u] = s + 4 + u < m ? __ldcs(lp + (size_t)(s + 4 + u) * stride) : 0;
         float4 l[4], g[4];
         X x[4];
 #pragma unroll
