@@ -131,6 +131,7 @@ int alloc_all(tsg_handle* h) {
     rc |= dalloc(h, &g.cell_of, n); rc |= dalloc(h, &g.rank, n); rc |= dalloc(h, &g.count, nb);
     rc |= dalloc(h, &g.cell_start, nb + 1); rc |= dalloc(h, &g.perm, n);
     rc |= dalloc(h, &g.tile_sum, nb / 2048 + 2);
+    rc |= dalloc(h, &g.big, cellsort_big_ints(n)); rc |= dalloc(h, &g.nbig, 1);
     rc |= dalloc(h, &g.list_flow, n + 1); rc |= dalloc(h, &g.list_bdy, n + 1);
     rc |= dalloc(h, &g.list_count, 2); rc |= dalloc(h, &g.err, 1);
     rc |= dalloc(h, &h->d_stage, 9 * n + 16);

@@ -37,6 +37,7 @@
 #include "tsg_fp32_dev.cuh"
 #include "tsg_polar.cuh"
 #include "tsg_rigid_list.cuh"
+#include "tsg_cellsort.cuh"
 
 namespace tsg {
 
@@ -70,18 +71,6 @@ __global__ void k_scatter32(int count_n, const int* __restrict__ cell_of, const 
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count_n) return;
     perm[cell_start[cell_of[t]] + rank[t]] = t;
-}
-
-__global__ void k_cell_sort32(long long ncell, const int* __restrict__ cell_start, int* __restrict__ perm) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    int b = cell_start[c], e = cell_start[c + 1];
-    for (int q = b + 1; q < e; ++q) {
-        int v = perm[q];
-        int m = q - 1;
-        while (m >= b && perm[m] > v) { perm[m + 1] = perm[m]; --m; }
-        perm[m + 1] = v;
-    }
 }
 
 // Gather block [base, base + count_n) from a into b (new order), renormalise hi/lo and
@@ -1924,7 +1913,7 @@ void build_cells(Fp32State& st, int base, int count_n, int* count, int* start, c
     TSG_LAUNCH(k_hash32, nblk(count_n), TPB, s, k, count_n, base, a.hi, a.lo, st.cell_of, st.rank, count, st.err);
     scan_exclusive(count, start, (int)nbins, st.tiles, s);
     TSG_LAUNCH(k_scatter32, nblk(count_n), TPB, s, count_n, st.cell_of, st.rank, start, st.perm);
-    TSG_LAUNCH(k_cell_sort32, nblk(nbins), TPB, s, nbins, start, st.perm);
+    sort_within_cells(nbins, start, st.cell_of, count_n, st.perm, st.sort_big, st.sort_nbig, s);
     P32& b = st.P[1 - st.cur];
     TSG_LAUNCH(k_reorder32, nblk(count_n), TPB, s, k, count_n, base, st.perm, a, b, st.pf);
     (void)reorder_into_next;
@@ -2052,11 +2041,13 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     st->ovf_list = dal<int>(*st, n); st->novf = dal<int>(*st, 1);
     st->sact = dal<int>(*st, n - nd > 0 ? n - nd : 1); st->nsact = dal<int>(*st, 1);
     st->maxdisp = dal<unsigned>(*st, 1);
+    st->sort_big = dal<int>(*st, cellsort_big_ints(n));
+    st->sort_nbig = dal<int>(*st, 1);
     st->d_rebuilds = dal<int>(*st, 1);
     st->cells_per_cta = c.dim == 3 ? 4 : 0;
     st->stage = dal<double>(*st, 9 * (size_t)n + 16);
     st->scratch = dal<double>(*st, 64);
-    if (!t.nbr || !st->stage) { fp32_destroy(st); return TSG_E_CUDA; }
+    if (!t.nbr || !st->stage || !st->sort_big || !st->sort_nbig) { fp32_destroy(st); return TSG_E_CUDA; }
     // upload raw arrays through the staging buffer, then split on the device
     double* dx = st->stage;                 // 3n
     double* dv = dx + 3 * (size_t)n;        // 3n

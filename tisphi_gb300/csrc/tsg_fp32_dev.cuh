@@ -634,6 +634,7 @@ struct Fp32State {
     int *r_ids = nullptr, *r_off = nullptr, *r_list = nullptr, *r_scratch = nullptr;
     double *r_q = nullptr, *r_part = nullptr, *r_cm = nullptr, *r_rot = nullptr;
     unsigned* maxdisp = nullptr;               // squared displacement since the last list build
+    int *sort_big = nullptr, *sort_nbig = nullptr;  // the cell sort's cells above kSortSmall particles
     bool built = false;
     double* stage = nullptr;       // f64 export staging (9 n)
     double* scratch = nullptr;

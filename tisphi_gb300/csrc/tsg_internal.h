@@ -60,6 +60,11 @@ struct Consts {
 // (from the uploaded positions, in upload order) and, per object, the slice of `list`
 // that the list builder (tsg_rigid_list.cuh) fills with the object's particles in
 // ascending order before every shape matching.
+// Largest cell segment the counting sort's last step gives to one thread (tsg_cellsort.cuh),
+// and the size of its list of larger cells (at most n / (kSortSmall + 1) of them).
+constexpr int kSortSmall = 256;
+inline size_t cellsort_big_ints(long long n) { return (size_t)(n / kSortSmall + 2); }
+
 // Block size of the rigid-object list builder (tsg_rigid_list.cuh) and its scratch size.
 constexpr int kRListBlock = 256;
 inline int rlist_blocks(int n) { return (n + kRListBlock - 1) / kRListBlock; }
@@ -127,6 +132,8 @@ struct Grid {
     int* list_bdy;      // boundary + rigid particles
     int* list_count;    // [0] flow, [1] bdy
     int* err;           // device error word
+    int* big;           // cells above kSortSmall particles (cellsort_big_ints)
+    int* nbig;          // their count
 };
 
 // ---- headless visual buffer (tsg_visual.cu) ----

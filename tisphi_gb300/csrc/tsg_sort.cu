@@ -10,12 +10,13 @@
 //   scan        exclusive prefix sum of the G + 1 counts (the extra bin collects
 //               particles whose flattened index falls outside [0, G));
 //   k_scatter   perm[cell_start + rank] = old index (unstable inside a cell);
-//   k_cell_sort insertion-sorts each cell's short segment by old index (stable result);
+//   sort_within_cells (tsg_cellsort.cuh) orders each cell by old index (stable result);
 //   k_reorder   gathers every persistent field into the other buffer set, writes the f32
 //               prefilter positions and the flow / boundary index lists.
 // Compiled with -fmad=false: the f64 cell arithmetic must round exactly like the oracle's.
 #include <cstdio>
 
+#include "tsg_cellsort.cuh"
 #include "tsg_internal.h"
 
 namespace tsg {
@@ -128,20 +129,6 @@ __global__ void k_scatter(int n, const int* __restrict__ cell_of, const int* __r
     perm[cell_start[cell_of[i]] + rank[i]] = i;
 }
 
-// Stable order inside each cell: ascending old index (the serial order of the reference's
-// counting sort).  Segments hold a few dozen entries, so one thread per cell suffices.
-__global__ void k_cell_sort(long long ncell, const int* __restrict__ cell_start, int* __restrict__ perm) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    int b = cell_start[c], e = cell_start[c + 1];
-    for (int k = b + 1; k < e; ++k) {
-        int v = perm[k];
-        int m = k - 1;
-        while (m >= b && perm[m] > v) { perm[m + 1] = perm[m]; --m; }
-        perm[m + 1] = v;
-    }
-}
-
 __device__ __forceinline__ void append(int* list, int* counter, bool pred, int value) {
     unsigned mask = __ballot_sync(0xffffffffu, pred);
     if (!mask) return;
@@ -218,7 +205,7 @@ void sort_fp64(const Consts& c, Persist64& cur, Persist64& nxt, Trans64& t, Grid
     TSG_LAUNCH(k_hash, nblk(c.n), TPB, s, c, cur.x, g.cell_of, g.rank, g.count, g.err);
     scan_exclusive(g.count, g.cell_start, (int)nbins, g.tile_sum, s);
     TSG_LAUNCH(k_scatter, nblk(c.n), TPB, s, c.n, g.cell_of, g.rank, g.cell_start, g.perm);
-    TSG_LAUNCH(k_cell_sort, nblk(nbins), TPB, s, nbins, g.cell_start, g.perm);
+    sort_within_cells(nbins, g.cell_start, g.cell_of, c.n, g.perm, g.big, g.nbig, s);
     if (c.solver == 1) {
         TSG_LAUNCH(k_reorder64<false>, nblk(c.n), TPB, s, c, g.perm, cur, nxt, t.pos32, g.list_flow, g.list_bdy,
                    g.list_count, nullptr, nullptr);
