@@ -10,8 +10,10 @@
 //   k_rlist_fill   every block writes its particles of each object at the object's slice
 //                  start off[o] + its block offset + its rank inside the block (warps in
 //                  order, lanes in order), so each slice comes out in ascending index.
-// Scratch: nobj * nblocks ints (rlist_scratch_ints, tsg_internal.h).  The slices off[o] .. off[o + 1] are
-// sized at upload from the same predicate, which no step changes.
+// Scratch: nobj * nblocks ints (rlist_scratch_ints, tsg_internal.h).  The slices
+// off[o] .. off[o + 1] are sized at upload from the same predicate, which no step changes.
+// The count and fill passes take one ballot round (two barriers) per object in every
+// block, so their cost grows with the number of dynamic bodies (scenes hold a few).
 #pragma once
 
 #include <cuda_runtime.h>
