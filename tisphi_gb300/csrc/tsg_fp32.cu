@@ -1014,6 +1014,24 @@ __global__ void k_bdy_soil32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
     });
 }
 
+// The stress and rho_tmp - rho0 of every particle packed for the stress-divergence pass's
+// neighbour reads: one 128-bit read per neighbour in 2D, (s_xx, s_yy, s_xy, rho~ - rho0), and
+// one 256-bit read in 3D, (s_xx, s_yy, s_zz, rho~ - rho0), (s_xy, s_xz, s_yz, 0), in place
+// of four / seven 32-bit reads from the planes.  Run right before that pass (after the
+// boundary extrapolation has written the dummies' values).
+template <int DIM>
+__global__ void k_pack_stress32(K32 k, T32 t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    const size_t n = k.n;
+    if (DIM == 2) {
+        t.srec[i] = make_float4(t.sigt[i], t.sigt[n + i], t.sigt[3 * n + i], t.drt[i]);
+    } else {
+        t.srec[2 * (size_t)i] = make_float4(t.sigt[i], t.sigt[n + i], t.sigt[2 * n + i], t.drt[i]);
+        t.srec[2 * (size_t)i + 1] = make_float4(t.sigt[3 * n + i], t.sigt[4 * n + i], t.sigt[5 * n + i], 0.f);
+    }
+}
+
 // Stress divergence + damping (mu(I), eng/solver_sph_muI.py:113-128), and for DP also the
 // velocity gradient, continuity and Bui-2008 stress rate (eng/solver_sph_dp.py:172-208,
 // :236-270), all in one traversal.
@@ -1038,20 +1056,24 @@ __global__ void k_soil_mom32(K32 k, P32 p, T32 t, const float4* __restrict__ PF,
         const bool rep_on = k.boundary == 3 || k.boundary == 4;
         for_nbrs<DIM, FB>(k, i, t.cnt, t.nbr, p.hi, p.lo, PF, dstart, sstart, true,
                           [&](int j, const float* d, float r2, int sidx, int tj, float mVj) {
-            const float rtj = k.rho0 + t.drt[j];
+            // the neighbour's stress and rho_tmp - rho0 in one packed read
+            float4 sa, sb = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (DIM == 2) sa = t.srec[j];
+            else ldg_rec(t.srec, j, sa, sb);
+            const float rtj = k.rho0 + sa.w;
             const float r = fast_sqrt(r2);
             float kc[3];
             grad_c<DIM, CORR>(L, w_grad(k, r), d, kc);
             const float irj = __fdividef(1.f, rtj * rtj);
             const float coef = mVj * rtj;
             // m_ab = sigma_j / rho_j^2 + sigma_i / rho_i^2
-            const float mxx = t.sigt[j] * irj + ai[0];
-            const float myy = t.sigt[n + j] * irj + ai[1];
-            const float mxy = t.sigt[3 * n + j] * irj + ai[3];
+            const float mxx = sa.x * irj + ai[0];
+            const float myy = sa.y * irj + ai[1];
+            const float mxy = (DIM == 2 ? sa.z : sb.x) * irj + ai[3];
             if (DIM == 3) {
-                const float mzz = t.sigt[2 * n + j] * irj + ai[2];
-                const float mxz = t.sigt[4 * n + j] * irj + ai[4];
-                const float myz = t.sigt[5 * n + j] * irj + ai[5];
+                const float mzz = sa.z * irj + ai[2];
+                const float mxz = sb.y * irj + ai[4];
+                const float myz = sb.z * irj + ai[5];
                 dv[0].add(coef * (mxx * kc[0] + mxy * kc[1] + mxz * kc[2]));
                 dv[1].add(coef * (mxy * kc[0] + myy * kc[1] + myz * kc[2]));
                 dv[2].add(coef * (mxz * kc[0] + myz * kc[1] + mzz * kc[2]));
@@ -2029,6 +2051,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     if (soil) {
         t.vtlo = dal<float4>(*st, n);
         t.sigt = dal<float>(*st, 6 * (size_t)n); t.dee = dal<float>(*st, n);
+        t.srec = dal<float4>(*st, 2 * (size_t)n);
         if (c.solver == 3) { t.dsig = dal<float>(*st, 6 * (size_t)n); t.deep = dal<float>(*st, n); }
     }
     st->pf = dal<float4>(*st, n);
@@ -2047,7 +2070,7 @@ int fp32_create(const tsg_config& cfg, const Consts& c, const tsg_particles* pp,
     st->cells_per_cta = c.dim == 3 ? 4 : 0;
     st->stage = dal<double>(*st, 9 * (size_t)n + 16);
     st->scratch = dal<double>(*st, 64);
-    if (!t.nbr || !st->stage || !st->sort_big || !st->sort_nbig) { fp32_destroy(st); return TSG_E_CUDA; }
+    if (!t.nbr || !st->stage || !st->sort_big || !st->sort_nbig || (soil && !t.srec)) { fp32_destroy(st); return TSG_E_CUDA; }
     // upload raw arrays through the staging buffer, then split on the device
     double* dx = st->stage;                 // 3n
     double* dv = dx + 3 * (size_t)n;        // 3n
@@ -2450,6 +2473,7 @@ void soil_one_step(Fp32State& st, cudaStream_t s) {
     }
     {
         PhaseScope ph(s, PH_RATES);
+        TSG_LAUNCH(k_pack_stress32<DIM>, nblk(k.n), TPB, s, k, st.T);
 #define SOIL_MOM(CORR, DP)                                                                                       \
         do {                                                                                                     \
             TSG_LAUNCH((k_soil_mom32<DIM, false, CORR, DP>), nb, st.tpb, s, k, p, st.T, st.pf, st.dstart, st.sstart, ovf); \

@@ -501,6 +501,7 @@ struct T32 {
     float* dee;     // d_strain_equ
     float* deep;    // d_strain_equ_p (Drucker-Prager)
     float4* vtlo;   // v_tmp low part (zero for dummies)
+    float4* srec;   // stress_tmp and rho_tmp - rho0 packed per particle (k_pack_stress32)
     // RK4 accumulators (time_integration 4 only)
     float* ddrk;
     float4* dvrk;
